@@ -1,0 +1,239 @@
+/* sop_gpu.h -- C ABI of the GB300 SOP engine (libsopgpu.so).
+ *
+ * One engine owns one CUDA device, one stream and all device memory of the
+ * systems ("replicas") admitted to it.  Every entry point returns an int
+ * status (SOP_OK or a negative SOP_ERR_*); no C++ exception crosses the ABI.
+ * An engine is driven by one host thread at a time.  Bead indices are 0-based
+ * in arrays; pair lists handed back use the reference's 1-based numbering.
+ *
+ * Reference interfaces replaced (SOP-CPU, file:line):
+ *   update_neighbor_list()        neighbor_list.cpp:6    -> sop_update_neighbor_list
+ *   update_cell_list()            cell_list.cpp:6        -> sop_update_cell_list
+ *   update_pair_list()            sop.cpp:473            -> sop_update_pair_list
+ *   force_eval() / set_forces()   energy.cpp:21, 78      -> sop_force_eval, sop_params.force_terms
+ *   energy_eval() / set_potential energy.cpp:6, 47       -> sop_energy_eval
+ *   underdamped_iteration(coord*) sop.cpp:282            -> sop_underdamped_iteration
+ *   calculate_observables(coord*) sop.cpp:200            -> sop_observables
+ *   underdamped_ctrl() step loop  sop.cpp:93-198         -> sop_run_plain (one system),
+ *                                                           sop_run (all systems, batched)
+ *   load bonds/angles/vdw/init    params.cpp:110-260     -> sop_replica_add (arrays)
+ *   set <keyword>                 params.cpp:12-101      -> sop_params
+ */
+#ifndef SOP_GPU_H
+#define SOP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define SOP_OK 0
+#define SOP_ERR_ARG -1         /* bad argument (null pointer, size, index)      */
+#define SOP_ERR_CUDA -2        /* a CUDA runtime call failed                    */
+#define SOP_ERR_NOMEM -3       /* device or host allocation failed              */
+#define SOP_ERR_STATE -4       /* call not valid in the current state           */
+#define SOP_ERR_OVERFLOW -5    /* a neighbor-list row or output buffer is full  */
+#define SOP_ERR_UNSUPPORTED -6 /* input outside what the engine implements      */
+#define SOP_ERR_NODEV -7       /* no usable CUDA device                         */
+#define SOP_ERR_REPLICA -8     /* a replica carries an error status (see below) */
+#define SOP_ERR_FULL -9        /* no room: admission refused, retry later        */
+
+/* per-replica status bits (sop_replica_status) */
+#define SOP_ST_NONFINITE 0x1     /* NaN/inf force or position                   */
+#define SOP_ST_FENE 0x2          /* a bond stretched to |d - r0| >= R0           */
+#define SOP_ST_LIST_OVERFLOW 0x4 /* a neighbor-list row overflowed; frozen       */
+#define SOP_ST_PERIODIC 0x8      /* extent reached boxl/2: images would apply    */
+#define SOP_ST_GRID 0x10         /* cell grid larger than the engine supports    */
+
+/* list modes: which pair search feeds the per-step pair-list filter */
+#define SOP_LIST_NONE 0     /* cutofftype unset: every candidate interacts     */
+#define SOP_LIST_NEIGHBOR 1 /* 3.2x neighbor list every nnlup steps (reference) */
+#define SOP_LIST_CELL 2     /* cell-adjacency screen every nnlup steps          */
+#define SOP_LIST_SKIN 3     /* Verlet list at 2.5x + skin, rebuilt on displacement */
+
+/* force terms (energy.cpp:78-113 switch slots 1, 2, 3, 6) */
+#define SOP_TERM_RANDOM 0x1
+#define SOP_TERM_FENE 0x2
+#define SOP_TERM_ANGLE 0x4
+#define SOP_TERM_VDW 0x8
+#define SOP_TERM_ALL 0xF
+
+/* integrator precision */
+#define SOP_PREC_MIXED 0 /* FP32 pair forces, FP64 positions (default)      */
+#define SOP_PREC_FP64 1  /* FP64 pair forces and update (drift reference)   */
+
+/* Run and force-field parameters of one system: the reference globals the
+ * hot path reads (params.cpp:262-400 defaults via sop_params_default). */
+typedef struct sop_params {
+  double T;       /* temperature, kcal/mol                                  */
+  double zeta;    /* friction                                               */
+  double h;       /* time step                                              */
+  double a1, a2, a3, a4; /* integrator constants (params.cpp:22-27, 84-98)  */
+  double boxl;    /* box edge for the minimum image                         */
+  double lcell;   /* cell edge of the cell-adjacency mode (boxl/ncell)      */
+  double ncell;   /* cells per box edge                                     */
+  double k_bnd, R0;          /* FENE (params.cpp:268-271)                    */
+  double sigma_ss, epsilon_ss; /* i,i+2 soft sphere (params.cpp:289-293)     */
+  double skin;    /* SOP_LIST_SKIN: list cutoff is 2.5 sigma + skin, A       */
+  double cell_edge; /* spatial-grid edge used by the list build, A (0=auto)  */
+  double pull_force; /* constant force on the two termini along their
+                        separation, kcal/mol/A (0 = off; no reference term)  */
+  uint64_t seed;  /* counter-based noise key                                */
+  int nnlup;      /* list update period in steps                            */
+  int nup;        /* output period in steps (energies, observables)         */
+  int list_mode;  /* SOP_LIST_*                                             */
+  int force_terms; /* SOP_TERM_* mask                                       */
+  int precision;  /* SOP_PREC_*                                             */
+  int pull_i, pull_j; /* pulled beads (default first and last)              */
+} sop_params;
+
+/* One system: topology + initial state.  All arrays 0-based, borrowed. */
+typedef struct sop_system_desc {
+  int nbead;
+  const double* xyz;       /* initial unc_pos, 3*nbead (pos = unc_pos)       */
+  const double* vel;       /* initial velocities or NULL (zero)              */
+  const int* bead_type;    /* 1 or 2 per bead, or NULL (all 1)               */
+  const int* chain;        /* chain id per bead, or NULL (one chain)         */
+  int nbnd; const int* ib; const int* jb; const double* r0;   /* FENE bonds  */
+  int nang; const int* ia; const int* ka;                     /* i,k of angles */
+  int nnat; const int* in_; const int* jn; const double* rn;  /* natives     */
+  /* Non-native candidates are implicit: every pair with chain[i]!=chain[j] or
+   * |i-j|>2 that is not native.  Pairs of that set that must NOT interact
+   * (a vdw file listing fewer candidates) are given here: */
+  int nexcl; const int* ie; const int* je;
+  sop_params params;
+} sop_system_desc;
+
+typedef struct sop_engine sop_engine;
+
+typedef struct sop_engine_config {
+  int device;            /* CUDA ordinal                                       */
+  int max_beads;         /* bead capacity of the packed arrays (0 = 1<<20)     */
+  int max_replicas;      /* replica slots (0 = 4096)                           */
+  int64_t max_list_entries; /* neighbor-list entry capacity (0 = 64 per bead)  */
+  int block_threads;     /* fused step kernel block size (0 = 256)            */
+  int lanes_per_bead;    /* lanes cooperating on one bead: 1,2,4,8 (0 = 4)     */
+  int graph_steps;       /* steps captured per CUDA graph launch (0 = 20)      */
+} sop_engine_config;
+
+/* ---- engine -------------------------------------------------------------- */
+const char* sop_version(void);
+const char* sop_status_string(int status);
+void sop_params_default(sop_params* p);   /* params.cpp:262-400 defaults      */
+void sop_engine_config_default(sop_engine_config* c);
+int sop_engine_create(const sop_engine_config* cfg, sop_engine** out);
+int sop_engine_destroy(sop_engine* e);
+int sop_engine_sync(sop_engine* e);
+/* bytes of device memory a system would take (admission by memory) */
+int sop_system_bytes(const sop_engine* e, const sop_system_desc* d, int64_t* bytes);
+int sop_engine_free_bytes(const sop_engine* e, int64_t* bytes);
+/* kernels launched by this engine since creation (all entry points) */
+int sop_engine_launches(const sop_engine* e, int64_t* launches);
+
+/* ---- replicas ------------------------------------------------------------- */
+/* Upload a system; builds its lists at the initial positions (the set-up of
+ * underdamped_ctrl, sop.cpp:117-125) and evaluates nothing else. */
+int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* replica);
+int sop_replica_remove(sop_engine* e, int replica);
+int sop_replica_set_params(sop_engine* e, int replica, const sop_params* p);
+int sop_replica_get_params(sop_engine* e, int replica, sop_params* p);
+/* host copies (any pointer may be NULL): wrapped pos, unc_pos, vel (3*nbead) */
+int sop_replica_get_state(sop_engine* e, int replica, double* pos, double* unc_pos, double* vel);
+/* overwrite unc_pos (and pos) and velocities; vel NULL = zero */
+int sop_replica_set_state(sop_engine* e, int replica, const double* unc_pos, const double* vel);
+int sop_replica_status(sop_engine* e, int replica, int* status, int64_t* steps_done);
+int sop_replica_count(const sop_engine* e, int* n);
+
+/* ---- reference-named operations on one replica (synchronous) -------------- */
+int sop_update_neighbor_list(sop_engine* e, int replica);   /* neighbor_list.cpp:6 */
+int sop_update_cell_list(sop_engine* e, int replica);       /* cell_list.cpp:6     */
+int sop_update_pair_list(sop_engine* e, int replica);       /* sop.cpp:473         */
+/* which: 0 neighbor att, 1 neighbor rep, 2 pair att, 3 pair rep.  Writes up to
+ * cap pairs (1-based, i<j) sorted by (i,j); *count gets the full count. */
+int sop_get_pair_list(sop_engine* e, int replica, int which, int* ii, int* jj, int cap, int* count);
+/* forces at the current positions with the current pair list (energy.cpp:21);
+ * the random term draws force evaluation number `noise_index` of the stream */
+int sop_force_eval(sop_engine* e, int replica, double* force_xyz);
+/* out[0..5] = e_bnd, e_ang_ss, e_vdw_rr, e_vdw_rr_att, e_vdw_rr_rep, rna_etot */
+int sop_energy_eval(sop_engine* e, int replica, double* out);
+/* one underdamped_iteration at the current pair list (sop.cpp:282-329) */
+int sop_underdamped_iteration(sop_engine* e, int replica);
+/* out[0..4] = Q, contct_nat, rgsq, kinT, end-to-end distance */
+int sop_observables(sop_engine* e, int replica, double* out);
+
+/* ---- stepping -------------------------------------------------------------- */
+/* The plain single-system path: the underdamped_ctrl loop for one replica,
+ * one kernel sequence per step, no graph, no batching. */
+int sop_run_plain(sop_engine* e, int replica, int64_t nsteps);
+/* All active replicas, packed into one persistent kernel per step, with
+ * per-replica rebuilds, the step loop captured in CUDA graphs. */
+int sop_run(sop_engine* e, int64_t nsteps);
+/* End-to-end call with HOST buffers (restart semantics, sop.cpp:132-147):
+ * load unc_pos/vel of every active replica (packed in replica-id order,
+ * 3*nbead each), evaluate the initial force, run nsteps, write them back. */
+int sop_run_host(sop_engine* e, const double* xyz_in, const double* vel_in, int64_t nsteps,
+                 double* xyz_out, double* vel_out);
+/* device time of the last sop_run (ms) and of its fused step kernels (ms) */
+int sop_last_run_timing(sop_engine* e, double* total_ms, double* step_kernel_ms,
+                        int64_t* step_kernel_launches);
+/* nsteps batched steps launched without a graph, with CUDA events around
+ * each kernel: mean device ms per launch of the fused step kernel and of the
+ * prologue (bookkeeping + list builds + output-step energies). */
+int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_kernel_ms, double* prologue_ms);
+
+/* ---- autotuner --------------------------------------------------------------- */
+/* Time the fused step for the active replicas over candidate block sizes,
+ * lanes per bead, cell edges and skins; adopt the fastest per size bucket.
+ * report (may be NULL) receives a text table of what was measured. */
+int sop_autotune(sop_engine* e, int steps_per_trial, char* report, int report_cap);
+
+/* ---- continuous-batching server ----------------------------------------------- */
+typedef struct sop_server sop_server;
+typedef struct sop_server_config {
+  sop_engine_config engine;
+  int max_active;          /* replica slots in flight (0 = 1024)              */
+  int64_t memory_budget;   /* device bytes admissions may use (0 = 80% free)  */
+  int chunk_steps;         /* steps between admission/retirement points (0=200) */
+} sop_server_config;
+typedef struct sop_request_result {
+  int64_t request_id;
+  int status;              /* SOP_OK or an error code                         */
+  int replica_status;
+  int nbead;
+  int64_t steps;
+  double submit_s, start_s, finish_s; /* server clock, seconds              */
+  double energy[6];        /* final energies (sop_energy_eval layout)         */
+  double observables[5];   /* final observables (sop_observables layout)      */
+} sop_request_result;
+int sop_server_create(const sop_server_config* cfg, sop_server** out);
+int sop_server_destroy(sop_server* s);
+/* queue a request; the desc arrays are copied. */
+int sop_server_submit(sop_server* s, const sop_system_desc* d, int64_t nsteps, int64_t* request_id);
+/* admit, advance one chunk, retire; returns the number of requests still
+ * queued or running in *pending. */
+int sop_server_pump(sop_server* s, int* pending);
+/* completed requests since the last call */
+int sop_server_poll(sop_server* s, sop_request_result* out, int cap, int* n);
+/* final state of a completed request (unc_pos 3*nbead); valid until polled twice */
+int sop_server_clock(sop_server* s, double* now_s);
+int sop_server_stats(sop_server* s, int64_t* bead_steps, int* active, int* queued);
+
+/* ---- synthetic systems (test and bench workloads) -------------------------------- */
+/* Seeded self-avoiding 3.8 A chain compacted by 2000-step-style minimisation. */
+int sop_synth_chain(uint64_t seed, int nbead, int compact_steps, double* xyz);
+/* nchain chains of chain_len beads packed into one globule. */
+int sop_synth_globule(uint64_t seed, int nchain, int chain_len, int compact_steps, double* xyz);
+
+/* ---- host-side numerics self-checks (no GPU needed) ------------------------------- */
+/* split a double into the (hi, lo) float pair the engine stages */
+void sop_selftest_split(double x, float* hi, float* lo);
+/* three Philox-4x32-10 normals as the step kernel draws them (host build) */
+void sop_selftest_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOP_GPU_H */

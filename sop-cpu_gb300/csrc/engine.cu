@@ -1,0 +1,1197 @@
+// Host side of the GB300 SOP engine: device memory, replica admission,
+// the plain and batched step loops, reference-named operations and the C ABI
+// declared in include/sop_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/sop_gpu.h"
+#include "engine.h"
+#include "kernels.cuh"
+#include "sop_common.cuh"
+
+namespace sop {
+
+// ---- force-field tables (global.cpp:60-92, params.cpp:281-286) ---------------
+
+static FFTables make_tables() {
+  FFTables t;
+  std::memset(&t, 0, sizeof t);
+  const double ca[3][3] = {{0, 0, 0}, {0, 0.7, 0.8}, {0, 0.8, 1.0}};
+  const double cr[3][3] = {{0, 0, 0}, {0, 1.0, 1.0}, {0, 1.0, 1.0}};
+  const double fa[3][3] = {{0, 0, 0}, {0, -12.0 * 1.0, -12.0 * 0.8}, {0, -12.0 * 0.8, -12.0 * 0.7}};
+  const double fr[3][3] = {{0, 0, 0}, {0, -6.0 * 1.0, -6.0 * 1.0}, {0, -6.0 * 1.0, -6.0 * 1.0}};
+  const double sr[3][3] = {{0, 0, 0}, {0, 3.8, 5.4}, {0, 5.4, 7.0}};
+  const double rn[3][3] = {{0, 0, 0}, {0, 8.0, 11.0}, {0, 11.0, 14.0}};
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      t.coeff_att[i][j] = ca[i][j];
+      t.coeff_rep[i][j] = cr[i][j];
+      t.force_coeff_att[i][j] = fa[i][j];
+      t.force_coeff_rep[i][j] = fr[i][j];
+      t.sigma_rep[i][j] = sr[i][j];
+      t.sigma_rep2[i][j] = sr[i][j] * sr[i][j];
+      t.sigma_rep6[i][j] = t.sigma_rep2[i][j] * t.sigma_rep2[i][j] * t.sigma_rep2[i][j];
+      t.sigma_rep12[i][j] = t.sigma_rep6[i][j] * t.sigma_rep6[i][j];
+      t.rcut_nat[i][j] = rn[i][j];
+      t.fca[i][j] = (float)fa[i][j];
+      t.fcr[i][j] = (float)fr[i][j];
+      t.s2[i][j] = (float)t.sigma_rep2[i][j];
+      double rpl = 2.5 * sr[i][j];  // sop.cpp:539-540
+      t.rc2_pl[i][j] = rpl * rpl;
+      double rnl = 3.2 * sr[i][j];  // neighbor_list.cpp:97-100
+      t.rc2_nl[i][j] = rnl * rnl;
+    }
+  return t;
+}
+
+const FFTables& tables() {
+  static FFTables t = make_tables();
+  return t;
+}
+
+// ---- first-fit range allocator ----------------------------------------------
+
+bool RangeAlloc::alloc(long long n, long long align, long long* out) {
+  if (n <= 0) { *out = 0; return true; }
+  for (auto it = free_.begin(); it != free_.end(); ++it) {
+    long long s = (it->first + align - 1) / align * align;
+    long long e = it->first + it->second;
+    if (s + n <= e) {
+      long long fs = it->first, fe = e;
+      free_.erase(it);
+      if (s > fs) free_[fs] = s - fs;
+      if (fe > s + n) free_[s + n] = fe - (s + n);
+      *out = s;
+      used_ += n;
+      return true;
+    }
+  }
+  return false;
+}
+
+void RangeAlloc::release(long long s, long long n) {
+  if (n <= 0) return;
+  used_ -= n;
+  auto it = free_.emplace(s, n).first;
+  auto nx = std::next(it);
+  if (nx != free_.end() && it->first + it->second == nx->first) {
+    it->second += nx->second;
+    free_.erase(nx);
+  }
+  if (it != free_.begin()) {
+    auto pv = std::prev(it);
+    if (pv->first + pv->second == it->first) {
+      pv->second += it->second;
+      free_.erase(it);
+    }
+  }
+}
+
+long long RangeAlloc::largest() const {
+  long long m = 0;
+  for (auto& kv : free_) m = std::max(m, kv.second);
+  return m;
+}
+
+}  // namespace sop
+
+using namespace sop;
+
+#define CK(call)                                                     \
+  do {                                                               \
+    cudaError_t e_ = (call);                                         \
+    if (e_ != cudaSuccess) {                                         \
+      std::snprintf(g_last_error, sizeof g_last_error, "%s: %s", #call, \
+                    cudaGetErrorString(e_));                         \
+      return SOP_ERR_CUDA;                                           \
+    }                                                                \
+  } while (0)
+
+static char g_last_error[512];
+
+// ---- defaults -------------------------------------------------------------------
+
+extern "C" const char* sop_version(void) { return "sop-gb300 1.0 (sm_103a)"; }
+
+extern "C" const char* sop_status_string(int s) {
+  switch (s) {
+    case SOP_OK: return "ok";
+    case SOP_ERR_ARG: return "bad argument";
+    case SOP_ERR_CUDA: return g_last_error[0] ? g_last_error : "CUDA error";
+    case SOP_ERR_NOMEM: return "out of memory";
+    case SOP_ERR_STATE: return "invalid state";
+    case SOP_ERR_OVERFLOW: return "list or buffer overflow";
+    case SOP_ERR_UNSUPPORTED: return "unsupported input";
+    case SOP_ERR_NODEV: return "no CUDA device";
+    case SOP_ERR_REPLICA: return "replica error status";
+    case SOP_ERR_FULL: return "engine full";
+    default: return "unknown";
+  }
+}
+
+static void set_integrator(sop_params* p, double h) {
+  // params.cpp:22-27 / 84-90 (set t_step)
+  p->h = h;
+  double halfh = h / 2.0;
+  p->a1 = h * (1.0 - p->zeta * halfh);
+  p->a2 = h * halfh;
+  p->a3 = (1.0 - h * p->zeta / 2.0 + (h * p->zeta) * (h * p->zeta) / 4.0) / h;
+  p->a4 = halfh * (1.0 - h * p->zeta / 2.0);
+}
+
+extern "C" void sop_params_default(sop_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  // params.cpp:262-400
+  p->T = 0.6;
+  p->zeta = 5.0e-2;
+  set_integrator(p, 2.5e-3);
+  p->boxl = 500.0;
+  p->ncell = 55.0;
+  p->lcell = p->boxl / p->ncell;
+  p->k_bnd = 20.0;
+  p->R0 = 2.0;
+  p->sigma_ss = 3.5;
+  p->epsilon_ss = 1.0;
+  p->skin = 2.0;
+  p->cell_edge = 0.0;
+  p->pull_force = 0.0;
+  p->seed = (uint64_t)(int64_t)(-101);  // set_seed(-100-run), run = 1
+  p->nnlup = 50;
+  p->nup = 1000;
+  p->list_mode = SOP_LIST_NEIGHBOR;
+  p->force_terms = SOP_TERM_ALL;
+  p->precision = SOP_PREC_MIXED;
+  p->pull_i = 0;
+  p->pull_j = -1;
+}
+
+extern "C" void sop_engine_config_default(sop_engine_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof *c);
+  c->device = 0;
+  c->max_beads = 1 << 21;
+  c->max_replicas = 4096;
+  c->max_list_entries = (int64_t)(1 << 21) * 64;
+  c->block_threads = 256;
+  c->lanes_per_bead = 4;
+  c->graph_steps = 20;
+}
+
+// ---- engine lifetime ------------------------------------------------------------
+
+template <class T>
+static cudaError_t dalloc(T** p, size_t n) {
+  return cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
+}
+
+extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** out) {
+  if (!out) return SOP_ERR_ARG;
+  *out = nullptr;
+  sop_engine_config cfg;
+  sop_engine_config_default(&cfg);
+  if (cfg_in) {
+    cfg.device = cfg_in->device;
+    if (cfg_in->max_beads > 0) cfg.max_beads = cfg_in->max_beads;
+    if (cfg_in->max_replicas > 0) cfg.max_replicas = cfg_in->max_replicas;
+    if (cfg_in->max_list_entries > 0) cfg.max_list_entries = cfg_in->max_list_entries;
+    if (cfg_in->block_threads > 0) cfg.block_threads = cfg_in->block_threads;
+    if (cfg_in->lanes_per_bead > 0) cfg.lanes_per_bead = cfg_in->lanes_per_bead;
+    if (cfg_in->graph_steps > 0) cfg.graph_steps = cfg_in->graph_steps;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    cudaGetLastError();
+    return SOP_ERR_NODEV;
+  }
+  if (cfg.device < 0 || cfg.device >= ndev) return SOP_ERR_ARG;
+  int lanes = cfg.lanes_per_bead;
+  if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16) return SOP_ERR_ARG;
+  if (cfg.block_threads % 32 || cfg.block_threads < 64 || cfg.block_threads > 256) return SOP_ERR_ARG;
+  std::unique_ptr<sop_engine> e(new (std::nothrow) sop_engine());
+  if (!e) return SOP_ERR_NOMEM;
+  e->cfg = cfg;
+  CK(cudaSetDevice(cfg.device));
+  CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  CK(cudaGetDeviceProperties(&e->prop, cfg.device));
+  const long long cap = cfg.max_beads;
+  const long long lcap = cfg.max_list_entries;
+  const long long ecap = cap * 24;  // native / bond / angle / exclusion entries
+  e->cap = cap;
+  DevArrays& A = e->A;
+  std::memset(&A, 0, sizeof A);
+  A.cap = cap;
+  for (int b = 0; b < 2; b++) {
+    CK(dalloc(&A.X[b], 3 * cap));
+    CK(dalloc(&A.stage[b], 2 * cap));
+  }
+  CK(dalloc(&A.incr, 3 * cap));
+  CK(dalloc(&A.vel, 3 * cap));
+  CK(dalloc(&A.force, 3 * cap));
+  CK(dalloc(&A.xb, cap));
+  CK(dalloc(&A.topo, cap));
+  CK(dalloc(&A.exc_rng, cap));
+  CK(dalloc(&A.nl_cnt, cap));
+  CK(dalloc(&A.nl, lcap));
+  CK(dalloc(&A.nat, ecap));
+  CK(dalloc(&A.nat_r0, ecap));
+  CK(dalloc(&A.bnd, cap * 4));
+  CK(dalloc(&A.bnd_r0, cap * 4));
+  CK(dalloc(&A.ang, cap * 4));
+  CK(dalloc(&A.exc, ecap));
+  CK(dalloc(&A.rep, cfg.max_replicas));
+  e->pairs_cap = 1 << 22;
+  CK(dalloc(&A.pairs_out, e->pairs_cap));
+  CK(dalloc(&A.pairs_cnt, 1));
+  CK(dalloc(&A.err, 1));
+  CK(cudaMemsetAsync(A.err, 0, sizeof(int), e->stream));
+  CK(cudaMemsetAsync(A.rep, 0, sizeof(RepDev) * cfg.max_replicas, e->stream));
+  CK(dalloc(&e->d_ids, cfg.max_replicas + 4));
+  CK(dalloc(&e->d_items, cap / 32 + cfg.max_replicas + 16));
+  e->items_cap = cap / 32 + cfg.max_replicas + 16;
+  CK(cudaMallocHost((void**)&e->h_rep, sizeof(RepDev)));
+  e->beads.init(cap);
+  e->lists.init(lcap);
+  e->nats.init(ecap);
+  e->bnds.init(cap * 4);
+  e->angs.init(cap * 4);
+  e->excs.init(ecap);
+  e->reps.resize(cfg.max_replicas);
+  upload_tables(tables(), e->stream);
+  CK(cudaGetLastError());
+  CK(init_kernels((int)e->prop.sharedMemPerBlockOptin));
+  for (int k = 0; k < 4; k++) CK(cudaEventCreate(&e->ev[k]));
+  CK(cudaStreamSynchronize(e->stream));
+  *out = e.release();
+  return SOP_OK;
+}
+
+extern "C" int sop_engine_destroy(sop_engine* e) {
+  if (!e) return SOP_ERR_ARG;
+  cudaSetDevice(e->cfg.device);
+  cudaStreamSynchronize(e->stream);
+  if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
+  DevArrays& A = e->A;
+  void* ptrs[] = {A.X[0], A.X[1], A.stage[0], A.stage[1], A.incr, A.vel, A.force, A.xb, A.topo,
+                  A.exc_rng, A.nl_cnt, A.nl, A.nat, A.nat_r0, A.bnd, A.bnd_r0, A.ang, A.exc,
+                  A.rep, A.pairs_out, A.pairs_cnt, A.err, e->d_ids, e->d_items};
+  for (void* p : ptrs) cudaFree(p);
+  if (e->h_rep) cudaFreeHost(e->h_rep);
+  for (int k = 0; k < 4; k++) if (e->ev[k]) cudaEventDestroy(e->ev[k]);
+  cudaStreamDestroy(e->stream);
+  delete e;
+  return SOP_OK;
+}
+
+extern "C" int sop_engine_sync(sop_engine* e) {
+  if (!e) return SOP_ERR_ARG;
+  CK(cudaStreamSynchronize(e->stream));
+  return SOP_OK;
+}
+
+extern "C" int sop_engine_launches(const sop_engine* e, int64_t* n) {
+  if (!e || !n) return SOP_ERR_ARG;
+  *n = e->launches;
+  return SOP_OK;
+}
+
+// ---- replica descriptors -------------------------------------------------------
+
+static int fill_repdev(const sop_params& p, RepDev& d) {
+  d.mode = p.list_mode;
+  d.terms = p.force_terms & SOP_TERM_ALL;
+  d.prec = p.precision;
+  d.nnlup = p.nnlup > 0 ? p.nnlup : 1;
+  d.nup = p.nup;
+  d.skin = (float)p.skin;
+  d.cell_edge = (float)p.cell_edge;
+  d.half_skin2 = (float)(0.25 * p.skin * p.skin);
+  d.boxl = p.boxl;
+  d.lcell = p.lcell;
+  d.ncell = p.ncell;
+  d.a1 = (float)p.a1; d.a2 = (float)p.a2; d.a3 = (float)p.a3; d.a4 = (float)p.a4;
+  d.a1d = p.a1; d.a2d = p.a2; d.a3d = p.a3; d.a4d = p.a4;
+  double amp = (p.h > 0 && p.T > 0 && p.zeta > 0) ? std::sqrt(2.0 * p.T * p.zeta / p.h) : 0.0;
+  d.noise_amp = (float)amp;  // random_force (energy.cpp:456)
+  d.T = (float)p.T;
+  if (p.T < kEpsT && p.T != 0.0) d.T = 0.0f;  // keep the sop.cpp:316 branch exact
+  d.kbnd = (float)p.k_bnd;
+  d.R0sq = (float)(p.R0 * p.R0);
+  d.kbnd_d = p.k_bnd;
+  d.R0sq_d = p.R0 * p.R0;
+  double s6 = std::pow(p.sigma_ss, 6.0);
+  d.e_ang_coeff = p.epsilon_ss * s6;
+  d.fang_d = 6.0 * d.e_ang_coeff;
+  d.fang = (float)d.fang_d;
+  d.e_bnd_coeff = p.k_bnd * (p.R0 * p.R0) / 2.0;
+  d.pull_f = (float)p.pull_force;
+  d.seed_lo = (uint32_t)p.seed;
+  d.seed_hi = (uint32_t)(p.seed >> 32);
+  if (p.list_mode < SOP_LIST_NONE || p.list_mode > SOP_LIST_SKIN) return SOP_ERR_ARG;
+  if (p.precision != SOP_PREC_MIXED) return SOP_ERR_UNSUPPORTED;
+  return SOP_OK;
+}
+
+// Exact count of list candidates per bead at the given positions, for sizing
+// the neighbor-list rows (same predicate as the device build, FP64).
+static int max_candidates(const sop_system_desc* d, const std::vector<int>& type,
+                          const std::vector<int>& chain, int mode) {
+  const int n = d->nbead;
+  if (mode == SOP_LIST_NONE) return n;
+  const double* x = d->xyz;
+  const FFTables& T = tables();
+  double rl = 0;
+  for (int a = 1; a < 3; a++)
+    for (int b = 1; b < 3; b++) {
+      double r = mode == SOP_LIST_SKIN ? 2.5 * T.sigma_rep[a][b] + d->params.skin
+                                       : 3.2 * T.sigma_rep[a][b];
+      rl = std::max(rl, r);
+    }
+  double edge = mode == SOP_LIST_CELL ? d->params.lcell : rl;
+  if (edge <= 0) return n;
+  std::unordered_map<long long, std::vector<int>> grid;
+  auto key = [](long long a, long long b, long long c) {
+    return ((a + (1 << 20)) << 42) ^ ((b + (1 << 20)) << 21) ^ (c + (1 << 20));
+  };
+  std::vector<long long> cx(n), cy(n), cz(n);
+  for (int i = 0; i < n; i++) {
+    cx[i] = (long long)std::floor(x[3 * i] / edge);
+    cy[i] = (long long)std::floor(x[3 * i + 1] / edge);
+    cz[i] = (long long)std::floor(x[3 * i + 2] / edge);
+    grid[key(cx[i], cy[i], cz[i])].push_back(i);
+  }
+  int best = 0;
+  for (int i = 0; i < n; i++) {
+    int cnt = 0;
+    for (int a = -1; a <= 1; a++)
+      for (int b = -1; b <= 1; b++)
+        for (int c = -1; c <= 1; c++) {
+          auto it = grid.find(key(cx[i] + a, cy[i] + b, cz[i] + c));
+          if (it == grid.end()) continue;
+          for (int j : it->second) {
+            if (j == i) continue;
+            if (chain[i] == chain[j] && std::abs(i - j) <= 2) continue;
+            if (mode == SOP_LIST_CELL) { cnt++; continue; }
+            double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1],
+                   dz = x[3 * j + 2] - x[3 * i + 2];
+            double r = mode == SOP_LIST_SKIN ? 2.5 * T.sigma_rep[type[i]][type[j]] + d->params.skin
+                                             : 3.2 * T.sigma_rep[type[i]][type[j]];
+            if (dx * dx + dy * dy + dz * dz < r * r) cnt++;
+          }
+        }
+    best = std::max(best, cnt);
+  }
+  return best;
+}
+
+struct Topo {
+  std::vector<int4> topo;
+  std::vector<int2> exc_rng;
+  std::vector<int4> nat;
+  std::vector<double> nat_r0;
+  std::vector<int4> bnd;
+  std::vector<double> bnd_r0;
+  std::vector<int> ang;
+  std::vector<int> exc;
+  std::vector<int> type, chain;
+  int nnat_pairs = 0;
+};
+
+static float f32_bits_float(float f) { return f; }
+
+static int build_topology(const sop_system_desc* d, Topo& T) {
+  const int n = d->nbead;
+  T.type.assign(n, 1);
+  T.chain.assign(n, 0);
+  for (int i = 0; i < n; i++) {
+    if (d->bead_type) {
+      if (d->bead_type[i] < 1 || d->bead_type[i] > 2) return SOP_ERR_UNSUPPORTED;
+      T.type[i] = d->bead_type[i];
+    }
+    if (d->chain) {
+      if (d->chain[i] < 0 || d->chain[i] >= (1 << 20)) return SOP_ERR_UNSUPPORTED;
+      T.chain[i] = d->chain[i];
+    }
+  }
+  const FFTables& F = tables();
+  std::vector<std::vector<std::pair<int, double>>> nat(n), bnd(n);
+  std::vector<std::vector<int>> ang(n), exc(n);
+  for (int k = 0; k < d->nnat; k++) {
+    int i = d->in_[k], j = d->jn[k];
+    if (i < 0 || j < 0 || i >= n || j >= n || i == j) return SOP_ERR_ARG;
+    // native iff r < rcut_nat (params.cpp:197); others stay non-native candidates
+    if (!(d->rn[k] < F.rcut_nat[T.type[i]][T.type[j]])) continue;
+    if (T.chain[i] == T.chain[j] && std::abs(i - j) <= 2) {
+      // the implicit candidate set excludes |i-j|<=2 on a chain; a native there
+      // is still honoured as a native pair (the vdw file may list it)
+    }
+    nat[i].push_back({j, d->rn[k]});
+    nat[j].push_back({i, d->rn[k]});
+    T.nnat_pairs++;
+  }
+  for (int k = 0; k < d->nbnd; k++) {
+    int i = d->ib[k], j = d->jb[k];
+    if (i < 0 || j < 0 || i >= n || j >= n || i == j) return SOP_ERR_ARG;
+    bnd[i].push_back({j, d->r0[k]});
+    bnd[j].push_back({i, d->r0[k]});
+  }
+  for (int k = 0; k < d->nang; k++) {
+    int i = d->ia[k], j = d->ka[k];
+    if (i < 0 || j < 0 || i >= n || j >= n || i == j) return SOP_ERR_ARG;
+    ang[i].push_back(j);
+    ang[j].push_back(i);
+  }
+  for (int k = 0; k < d->nexcl; k++) {
+    int i = d->ie[k], j = d->je[k];
+    if (i < 0 || j < 0 || i >= n || j >= n || i == j) return SOP_ERR_ARG;
+    exc[i].push_back(j);
+    exc[j].push_back(i);
+  }
+  T.topo.resize(n);
+  T.exc_rng.resize(n);
+  for (int i = 0; i < n; i++) {
+    auto& v = nat[i];
+    std::stable_sort(v.begin(), v.end(), [](auto& a, auto& b) { return a.first < b.first; });
+    for (size_t q = 1; q < v.size(); q++)
+      if (v[q].first == v[q - 1].first) return SOP_ERR_UNSUPPORTED;  // duplicate native pair
+    std::sort(exc[i].begin(), exc[i].end());
+    exc[i].erase(std::unique(exc[i].begin(), exc[i].end()), exc[i].end());
+    if (v.size() > 0xFFFF || bnd[i].size() > 0xFF || ang[i].size() > 0xFF) return SOP_ERR_UNSUPPORTED;
+    int4 t;
+    t.x = (int)T.nat.size();
+    t.y = (int)T.bnd.size();
+    t.z = (int)T.ang.size();
+    t.w = (int)v.size() | ((int)bnd[i].size() << 16) | ((int)ang[i].size() << 24);
+    T.topo[i] = t;
+    for (auto& pr : v) {
+      // r0^2 as a two-float pair so r0^2 - d^2 keeps precision near the minimum
+      double r0 = pr.second, r0sq = r0 * r0;
+      float hi = (float)r0sq, lo = (float)(r0sq - (double)hi), r0f = (float)r0;
+      int4 e;
+      e.x = pr.first;
+      std::memcpy(&e.y, &hi, 4);
+      std::memcpy(&e.z, &lo, 4);
+      std::memcpy(&e.w, &r0f, 4);
+      T.nat.push_back(e);
+      T.nat_r0.push_back(pr.second);
+    }
+    for (auto& pr : bnd[i]) {
+      double r0 = pr.second, r0sq = r0 * r0;
+      float r0f = (float)r0, hi = (float)r0sq, lo = (float)(r0sq - (double)hi);
+      int4 b;
+      b.x = pr.first;
+      std::memcpy(&b.y, &r0f, 4);
+      std::memcpy(&b.z, &hi, 4);
+      std::memcpy(&b.w, &lo, 4);
+      T.bnd.push_back(b);
+      T.bnd_r0.push_back(r0);
+    }
+    for (int j : ang[i]) T.ang.push_back(j);
+    T.exc_rng[i] = make_int2((int)T.exc.size(), (int)exc[i].size());
+    for (int j : exc[i]) T.exc.push_back(j);
+  }
+  (void)f32_bits_float;
+  return SOP_OK;
+}
+
+static int compute_L(const sop_system_desc* d, const Topo& T, int mode) {
+  if (mode == SOP_LIST_NONE) return (d->nbead + 7) / 8 * 8 + 8;
+  int m = max_candidates(d, T.type, T.chain, mode);
+  int L = m + m / 2 + 32;
+  return (L + 7) / 8 * 8;
+}
+
+extern "C" int sop_system_bytes(const sop_engine* e, const sop_system_desc* d, int64_t* bytes) {
+  if (!e || !d || !bytes || d->nbead <= 0) return SOP_ERR_ARG;
+  Topo T;
+  int rc = build_topology(d, T);
+  if (rc) return rc;
+  long long L = compute_L(d, T, d->params.list_mode);
+  long long n = d->nbead;
+  long long b = n * (2 * 24 + 2 * 32 + 12 + 24 + 24 + 16 + 16 + 8 + 4) + n * L * 4 +
+                (long long)T.nat.size() * 16 + (long long)T.bnd.size() * 24 +
+                (long long)T.ang.size() * 4 + (long long)T.exc.size() * 4;
+  *bytes = b;
+  return SOP_OK;
+}
+
+extern "C" int sop_engine_free_bytes(const sop_engine* e, int64_t* bytes) {
+  if (!e || !bytes) return SOP_ERR_ARG;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return SOP_ERR_CUDA;
+  *bytes = (int64_t)fr;
+  return SOP_OK;
+}
+
+template <class T>
+static cudaError_t h2d(T* dst, const T* src, size_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  return cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+int sop::upload_positions(sop_engine* e, int r, const double* xyz, int which_bufs) {
+  Replica& R = e->reps[r];
+  const int n = R.n;
+  const long long off = R.off, cap = e->cap;
+  std::vector<double> soa(3 * (size_t)n);
+  std::vector<float4> st(2 * (size_t)n);
+  for (int i = 0; i < n; i++) {
+    for (int c = 0; c < 3; c++) soa[(size_t)c * n + i] = xyz[3 * i + c];
+    float h[3], l[3];
+    for (int c = 0; c < 3; c++) split_double(xyz[3 * i + c], h[c], l[c]);
+    st[2 * i] = make_float4(h[0], h[1], h[2], (float)R.type[i]);
+    st[2 * i + 1] = make_float4(l[0], l[1], l[2], (float)R.chain[i]);
+  }
+  for (int b = 0; b < 2; b++) {
+    if (!(which_bufs & (1 << b))) continue;
+    for (int c = 0; c < 3; c++) CK(h2d(e->A.X[b] + c * cap + off, soa.data() + (size_t)c * n, n, e->stream));
+    CK(h2d(e->A.stage[b] + 2 * off, st.data(), 2 * (size_t)n, e->stream));
+  }
+  CK(cudaStreamSynchronize(e->stream));
+  return SOP_OK;
+}
+
+int sop::upload_velocities(sop_engine* e, int r, const double* vel) {
+  Replica& R = e->reps[r];
+  const int n = R.n;
+  const long long off = R.off, cap = e->cap;
+  std::vector<double> soa(3 * (size_t)n, 0.0);
+  std::vector<float> zero(3 * (size_t)n, 0.0f);
+  if (vel)
+    for (int i = 0; i < n; i++)
+      for (int c = 0; c < 3; c++) soa[(size_t)c * n + i] = vel[3 * i + c];
+  for (int c = 0; c < 3; c++) {
+    CK(h2d(e->A.vel + c * cap + off, soa.data() + (size_t)c * n, n, e->stream));
+    CK(h2d(e->A.incr + c * cap + off, zero.data() + (size_t)c * n, n, e->stream));
+  }
+  CK(cudaStreamSynchronize(e->stream));
+  return SOP_OK;
+}
+
+// Copy the device descriptor of replica r to the host mirror and back.
+int sop::get_rep(sop_engine* e, int r, RepDev* out) {
+  CK(cudaMemcpyAsync(e->h_rep, e->A.rep + r, sizeof(RepDev), cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  *out = *e->h_rep;
+  return SOP_OK;
+}
+
+int sop::put_rep(sop_engine* e, int r, const RepDev& d) {
+  *e->h_rep = d;
+  CK(cudaMemcpyAsync(e->A.rep + r, e->h_rep, sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return SOP_OK;
+}
+
+static bool live(const sop_engine* e, int r) {
+  return r >= 0 && r < (int)e->reps.size() && e->reps[r].live;
+}
+
+// Build the lists of replica r from its current positions (single CTA).
+int sop::build_now(sop_engine* e, int r, int mode) {
+  Replica& R = e->reps[r];
+  if (R.n > kBuildMax) return SOP_ERR_UNSUPPORTED;
+  int id = r;
+  CK(cudaMemcpyAsync(e->d_ids + scratch_id(e, 0), &id, sizeof(int), cudaMemcpyHostToDevice,
+                     e->stream));
+  CK(launch_prologue(e->A, e->d_ids + scratch_id(e, 0), 1, R.n, 1, mode, 1, e->stream));
+  e->launches++;
+  CK(cudaStreamSynchronize(e->stream));
+  return SOP_OK;
+}
+
+extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* replica) {
+  if (!e || !d || !replica || d->nbead <= 0 || !d->xyz) return SOP_ERR_ARG;
+  if ((d->nbnd && (!d->ib || !d->jb || !d->r0)) || (d->nang && (!d->ia || !d->ka)) ||
+      (d->nnat && (!d->in_ || !d->jn || !d->rn)) || (d->nexcl && (!d->ie || !d->je)))
+    return SOP_ERR_ARG;
+  if (d->nbead > kBuildMax) return SOP_ERR_UNSUPPORTED;
+  for (long long q = 0; q < 3LL * d->nbead; q++)
+    if (!std::isfinite(d->xyz[q])) return SOP_ERR_ARG;
+  RepDev rd;
+  std::memset(&rd, 0, sizeof rd);
+  int rc = fill_repdev(d->params, rd);
+  if (rc) return rc;
+  Topo T;
+  rc = build_topology(d, T);
+  if (rc) return rc;
+  int slot = -1;
+  for (int k = 0; k < (int)e->reps.size(); k++)
+    if (!e->reps[k].live) { slot = k; break; }
+  if (slot < 0) return SOP_ERR_FULL;
+  const int n = d->nbead;
+  const int L = compute_L(d, T, d->params.list_mode);
+  long long off, nlb, nb, bb, ab, xb;
+  if (!e->beads.alloc(n, 8, &off)) return SOP_ERR_FULL;
+  if (!e->lists.alloc((long long)n * L, 8, &nlb)) { e->beads.release(off, n); return SOP_ERR_FULL; }
+  if (!e->nats.alloc((long long)T.nat.size(), 1, &nb) || !e->bnds.alloc((long long)T.bnd.size(), 1, &bb) ||
+      !e->angs.alloc((long long)T.ang.size(), 1, &ab) || !e->excs.alloc((long long)T.exc.size(), 1, &xb)) {
+    // partial allocations are returned below via a temporary replica record
+    e->beads.release(off, n);
+    e->lists.release(nlb, (long long)n * L);
+    return SOP_ERR_FULL;
+  }
+  Replica& R = e->reps[slot];
+  R = Replica();
+  R.live = true;
+  R.n = n;
+  R.off = off;
+  R.nl_base = nlb;
+  R.L = L;
+  R.nat_base = nb; R.nnat_e = (long long)T.nat.size();
+  R.bnd_base = bb; R.nbnd_e = (long long)T.bnd.size();
+  R.ang_base = ab; R.nang_e = (long long)T.ang.size();
+  R.exc_base = xb; R.nexc_e = (long long)T.exc.size();
+  R.params = d->params;
+  R.type = T.type;
+  R.chain = T.chain;
+  R.nnat_pairs = T.nnat_pairs;
+  // rebase the per-bead ranges onto the arenas
+  for (int i = 0; i < n; i++) {
+    T.topo[i].x += (int)nb;
+    T.topo[i].y += (int)bb;
+    T.topo[i].z += (int)ab;
+    T.exc_rng[i].x += (int)xb;
+  }
+  if (nb + (long long)T.nat.size() > 0x7fffffffLL) return SOP_ERR_FULL;
+  CK(h2d(e->A.topo + off, T.topo.data(), n, e->stream));
+  CK(h2d(e->A.exc_rng + off, T.exc_rng.data(), n, e->stream));
+  CK(h2d(e->A.nat + nb, T.nat.data(), T.nat.size(), e->stream));
+  CK(h2d(e->A.nat_r0 + nb, T.nat_r0.data(), T.nat_r0.size(), e->stream));
+  CK(h2d(e->A.bnd + bb, T.bnd.data(), T.bnd.size(), e->stream));
+  CK(h2d(e->A.bnd_r0 + bb, T.bnd_r0.data(), T.bnd_r0.size(), e->stream));
+  CK(h2d(e->A.ang + ab, T.ang.data(), T.ang.size(), e->stream));
+  CK(h2d(e->A.exc + xb, T.exc.data(), T.exc.size(), e->stream));
+  CK(cudaMemsetAsync(e->A.nl_cnt + off, 0, sizeof(int) * n, e->stream));
+  rd.off = (int)off;
+  rd.n = n;
+  rd.nl_base = nlb;
+  rd.L = L;
+  rd.nat_base = (int)nb; rd.bnd_base = (int)bb; rd.ang_base = (int)ab; rd.exc_base = (int)xb;
+  int pi = d->params.pull_i, pj = d->params.pull_j;
+  rd.pull_i = (pi >= 0 && pi < n) ? pi : 0;
+  rd.pull_j = (pj >= 0 && pj < n) ? pj : n - 1;
+  rd.t = 0;
+  rd.cur = 0;
+  rd.inlup = 1;
+  rd.active = 1;
+  rc = put_rep(e, slot, rd);
+  if (rc) return rc;
+  rc = upload_positions(e, slot, d->xyz, 3);
+  if (rc) return rc;
+  rc = upload_velocities(e, slot, d->vel);
+  if (rc) return rc;
+  // set-up of underdamped_ctrl (sop.cpp:117-125): lists at the initial positions
+  rc = build_now(e, slot, d->params.list_mode);
+  if (rc) return rc;
+  e->layout_dirty = true;
+  *replica = slot;
+  return SOP_OK;
+}
+
+extern "C" int sop_replica_remove(sop_engine* e, int r) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  CK(cudaStreamSynchronize(e->stream));
+  Replica& R = e->reps[r];
+  RepDev d;
+  std::memset(&d, 0, sizeof d);
+  int rc = put_rep(e, r, d);
+  if (rc) return rc;
+  e->beads.release(R.off, R.n);
+  e->lists.release(R.nl_base, (long long)R.n * R.L);
+  e->nats.release(R.nat_base, R.nnat_e);
+  e->bnds.release(R.bnd_base, R.nbnd_e);
+  e->angs.release(R.ang_base, R.nang_e);
+  e->excs.release(R.exc_base, R.nexc_e);
+  R = Replica();
+  e->layout_dirty = true;
+  return SOP_OK;
+}
+
+extern "C" int sop_replica_count(const sop_engine* e, int* n) {
+  if (!e || !n) return SOP_ERR_ARG;
+  int c = 0;
+  for (auto& R : e->reps) c += R.live;
+  *n = c;
+  return SOP_OK;
+}
+
+extern "C" int sop_replica_set_params(sop_engine* e, int r, const sop_params* p) {
+  if (!e || !p || !live(e, r)) return SOP_ERR_ARG;
+  RepDev d;
+  int rc = get_rep(e, r, &d);
+  if (rc) return rc;
+  RepDev cfg = d;
+  rc = fill_repdev(*p, cfg);
+  if (rc) return rc;
+  Replica& R = e->reps[r];
+  bool mode_changed = cfg.mode != d.mode || p->skin != R.params.skin;
+  // configuration fields only; run state and layout stay
+  d.mode = cfg.mode; d.terms = cfg.terms; d.prec = cfg.prec; d.nnlup = cfg.nnlup; d.nup = cfg.nup;
+  d.skin = cfg.skin; d.cell_edge = cfg.cell_edge; d.half_skin2 = cfg.half_skin2;
+  d.boxl = cfg.boxl; d.lcell = cfg.lcell; d.ncell = cfg.ncell;
+  d.a1 = cfg.a1; d.a2 = cfg.a2; d.a3 = cfg.a3; d.a4 = cfg.a4;
+  d.a1d = cfg.a1d; d.a2d = cfg.a2d; d.a3d = cfg.a3d; d.a4d = cfg.a4d;
+  d.noise_amp = cfg.noise_amp; d.T = cfg.T; d.kbnd = cfg.kbnd; d.R0sq = cfg.R0sq;
+  d.kbnd_d = cfg.kbnd_d; d.R0sq_d = cfg.R0sq_d; d.fang = cfg.fang; d.fang_d = cfg.fang_d;
+  d.e_bnd_coeff = cfg.e_bnd_coeff; d.e_ang_coeff = cfg.e_ang_coeff; d.pull_f = cfg.pull_f;
+  d.seed_lo = cfg.seed_lo; d.seed_hi = cfg.seed_hi;
+  int pi = p->pull_i, pj = p->pull_j;
+  d.pull_i = (pi >= 0 && pi < R.n) ? pi : 0;
+  d.pull_j = (pj >= 0 && pj < R.n) ? pj : R.n - 1;
+  R.params = *p;
+  rc = put_rep(e, r, d);
+  if (rc) return rc;
+  if (mode_changed) {
+    // a new list mode may need longer rows than the replica holds
+    if (p->list_mode == SOP_LIST_NONE && R.L < R.n) return SOP_ERR_UNSUPPORTED;
+    rc = build_now(e, r, p->list_mode);
+  }
+  e->graph_valid = false;
+  return rc;
+}
+
+extern "C" int sop_replica_get_params(sop_engine* e, int r, sop_params* p) {
+  if (!e || !p || !live(e, r)) return SOP_ERR_ARG;
+  *p = e->reps[r].params;
+  return SOP_OK;
+}
+
+extern "C" int sop_replica_get_state(sop_engine* e, int r, double* pos, double* unc_pos,
+                                     double* vel) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  RepDev d;
+  int rc = get_rep(e, r, &d);
+  if (rc) return rc;
+  Replica& R = e->reps[r];
+  const int n = R.n;
+  const long long off = R.off, cap = e->cap;
+  std::vector<double> soa(3 * (size_t)n);
+  if (pos || unc_pos) {
+    for (int c = 0; c < 3; c++)
+      CK(cudaMemcpyAsync(soa.data() + (size_t)c * n, e->A.X[d.cur] + c * cap + off,
+                         n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    for (int i = 0; i < n; i++)
+      for (int c = 0; c < 3; c++) {
+        double u = soa[(size_t)c * n + i];
+        if (unc_pos) unc_pos[3 * i + c] = u;
+        if (pos) {
+          // wrapped coordinate (sop.cpp:300-302); equal to unc_pos inside the box
+          double b = d.boxl;
+          double t = u / b;
+          double rn = (t > 0) ? std::floor(t + 0.5) : std::ceil(t - 0.5);
+          pos[3 * i + c] = u - b * rn;
+        }
+      }
+  }
+  if (vel) {
+    for (int c = 0; c < 3; c++)
+      CK(cudaMemcpyAsync(soa.data() + (size_t)c * n, e->A.vel + c * cap + off, n * sizeof(double),
+                         cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    for (int i = 0; i < n; i++)
+      for (int c = 0; c < 3; c++) vel[3 * i + c] = soa[(size_t)c * n + i];
+  }
+  return SOP_OK;
+}
+
+extern "C" int sop_replica_set_state(sop_engine* e, int r, const double* unc_pos, const double* vel) {
+  if (!e || !live(e, r) || !unc_pos) return SOP_ERR_ARG;
+  RepDev d;
+  int rc = get_rep(e, r, &d);
+  if (rc) return rc;
+  if (d.running) return SOP_ERR_STATE;
+  rc = upload_positions(e, r, unc_pos, 3);
+  if (rc) return rc;
+  rc = upload_velocities(e, r, vel);
+  if (rc) return rc;
+  return SOP_OK;
+}
+
+extern "C" int sop_replica_status(sop_engine* e, int r, int* status, int64_t* steps) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  RepDev d;
+  int rc = get_rep(e, r, &d);
+  if (rc) return rc;
+  int err = 0;
+  CK(cudaMemcpy(&err, e->A.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (status) *status = d.status | (err ? 0x100 : 0);
+  if (steps) *steps = d.t;
+  return SOP_OK;
+}
+
+// ---- layout of the batched step -------------------------------------------------
+
+int sop::refresh_layout(sop_engine* e) {
+  if (!e->layout_dirty) return SOP_OK;
+  std::vector<int> ids;
+  for (int r = 0; r < (int)e->reps.size(); r++)
+    if (e->reps[r].live) ids.push_back(r);
+  std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return e->reps[a].n > e->reps[b].n; });
+  e->active = ids;
+  e->max_n = 0;
+  e->max_staged = 0;
+  e->items.clear();
+  const int chunk = e->chunk_beads;
+  for (int r : ids) {
+    const Replica& R = e->reps[r];
+    e->max_n = std::max(e->max_n, R.n);
+    const int staged = R.n <= kStageMax;
+    if (staged) e->max_staged = std::max(e->max_staged, R.n);
+    for (int b = 0; b < R.n; b += chunk) e->items.push_back(StepItem{r, b, std::min(R.n, b + chunk), staged});
+  }
+  if ((long long)e->items.size() > e->items_cap) return SOP_ERR_FULL;
+  if (!ids.empty()) CK(h2d(e->d_ids, ids.data(), ids.size(), e->stream));
+  if (!e->items.empty()) CK(h2d(e->d_items, e->items.data(), e->items.size(), e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  // persistent grid: as many CTAs as fit at once, at most one per item
+  const int per_sm = step_blocks_per_sm(e->cfg.lanes_per_bead, e->cfg.block_threads, e->max_staged);
+  e->step_grid = std::max(1, std::min((int)e->items.size(), per_sm * e->prop.multiProcessorCount));
+  e->pro_grid = std::max(1, std::min((int)ids.size(), e->prop.multiProcessorCount * 2));
+  e->layout_dirty = false;
+  e->graph_valid = false;
+  return SOP_OK;
+}
+
+// One batched step: prologue (+ builds, energies, observables) then the step kernel.
+int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items,
+                      int nitems, int max_n, int max_staged, int step_grid, int pro_grid) {
+  CK(launch_prologue(e->A, d_ids, nrep, max_n, 0, 0, pro_grid, e->stream));
+  CK(launch_step(e->A, d_items, nitems, max_staged, e->cfg.lanes_per_bead, e->cfg.block_threads,
+                 step_grid, e->stream));
+  e->launches += 2;
+  return SOP_OK;
+}
+
+__global__ void k_begin(RepDev* rep, const int* ids, int nrep, long long nsteps) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nrep) return;
+  RepDev* R = &rep[ids[k]];
+  if (!R->active) return;
+  R->t_end = R->t + nsteps;
+  R->first_pending = 1;
+  R->running = 1;
+}
+
+__global__ void k_set_phase(RepDev* rep, int r, int phase) {
+  RepDev* R = &rep[r];
+  R->phase = phase;
+  R->t_cur = R->t;
+  R->out = 0;
+}
+
+static int check_errors(sop_engine* e) {
+  int err = 0;
+  CK(cudaMemcpyAsync(&err, e->A.err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return err ? SOP_ERR_CUDA : SOP_OK;
+}
+
+// ---- plain single-system path ------------------------------------------------------
+
+extern "C" int sop_run_plain(sop_engine* e, int r, int64_t nsteps) {
+  if (!e || !live(e, r) || nsteps < 0) return SOP_ERR_ARG;
+  if (nsteps == 0) return SOP_OK;
+  Replica& R = e->reps[r];
+  CK(cudaSetDevice(e->cfg.device));
+  // per-replica id and items (kept at the top of the id / item arrays)
+  const int id_slot = scratch_id(e, 1);
+  std::vector<StepItem> items;
+  const int staged = R.n <= kStageMax;
+  for (int b = 0; b < R.n; b += e->chunk_beads) items.push_back(StepItem{r, b, std::min(R.n, b + e->chunk_beads), staged});
+  const long long item_slot = e->items_cap - (long long)items.size();
+  if (item_slot < (long long)e->items.size()) return SOP_ERR_FULL;
+  CK(cudaMemcpyAsync(e->d_ids + id_slot, &r, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  CK(h2d(e->d_items + item_slot, items.data(), items.size(), e->stream));
+  k_begin<<<1, 32, 0, e->stream>>>(e->A.rep, e->d_ids + id_slot, 1, nsteps);
+  e->launches++;
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(e->ev[0], e->stream));
+  const int grid = std::min((int)items.size(), 4 * e->prop.multiProcessorCount);
+  for (int64_t s = 0; s <= nsteps; s++) {
+    int rc = enqueue_step(e, e->d_ids + id_slot, 1, e->d_items + item_slot, (int)items.size(), R.n,
+                          staged ? R.n : 0, grid, 1);
+    if (rc) return rc;
+  }
+  CK(launch_observables(e->A, e->d_ids + id_slot, 1, e->stream));
+  e->launches++;
+  CK(cudaEventRecord(e->ev[1], e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]);
+  e->last_total_ms = ms;
+  e->last_step_ms = -1;
+  e->last_step_launches = nsteps + 1;
+  return check_errors(e);
+}
+
+// ---- batched path: all replicas, graph-captured chunks ------------------------------
+
+static int capture_graph(sop_engine* e) {
+  if (e->graph_valid) return SOP_OK;
+  if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  int64_t before = e->launches;
+  for (int s = 0; s < e->cfg.graph_steps; s++) {
+    int rc = enqueue_step(e, e->d_ids, (int)e->active.size(), e->d_items, (int)e->items.size(),
+                          e->max_n, e->max_staged, e->step_grid, e->pro_grid);
+    if (rc) { cudaStreamEndCapture(e->stream, &g); return rc; }
+  }
+  e->launches = before;  // counted when replayed
+  CK(cudaStreamEndCapture(e->stream, &g));
+  CK(cudaGraphInstantiate(&e->graph_exec, g, 0));
+  cudaGraphDestroy(g);
+  e->graph_valid = true;
+  return SOP_OK;
+}
+
+int sop::run_batched(sop_engine* e, int64_t nsteps, bool timed) {
+  int rc = refresh_layout(e);
+  if (rc) return rc;
+  if (e->active.empty() || nsteps <= 0) return SOP_OK;
+  rc = capture_graph(e);
+  if (rc) return rc;
+  const int nrep = (int)e->active.size();
+  k_begin<<<(nrep + 127) / 128, 128, 0, e->stream>>>(e->A.rep, e->d_ids, nrep, nsteps);
+  e->launches++;
+  CK(cudaGetLastError());
+  if (timed) CK(cudaEventRecord(e->ev[0], e->stream));
+  const int64_t iters = nsteps + 1;
+  const int S = e->cfg.graph_steps;
+  const int64_t full = iters / S;
+  for (int64_t k = 0; k < full; k++) {
+    CK(cudaGraphLaunch(e->graph_exec, e->stream));
+    e->launches += 2 * S;
+  }
+  for (int64_t k = full * S; k < iters; k++) {
+    rc = enqueue_step(e, e->d_ids, nrep, e->d_items, (int)e->items.size(), e->max_n, e->max_staged,
+                      e->step_grid, e->pro_grid);
+    if (rc) return rc;
+  }
+  CK(launch_observables(e->A, e->d_ids, nrep, e->stream));
+  e->launches++;
+  if (timed) CK(cudaEventRecord(e->ev[1], e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  if (timed) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]);
+    e->last_total_ms = ms;
+  }
+  e->last_step_launches = iters;
+  return check_errors(e);
+}
+
+extern "C" int sop_run(sop_engine* e, int64_t nsteps) {
+  if (!e || nsteps < 0) return SOP_ERR_ARG;
+  CK(cudaSetDevice(e->cfg.device));
+  return run_batched(e, nsteps, true);
+}
+
+extern "C" int sop_last_run_timing(sop_engine* e, double* total_ms, double* step_ms,
+                                   int64_t* step_launches) {
+  if (!e) return SOP_ERR_ARG;
+  if (total_ms) *total_ms = e->last_total_ms;
+  if (step_ms) *step_ms = e->last_step_ms;
+  if (step_launches) *step_launches = e->last_step_launches;
+  return SOP_OK;
+}
+
+extern "C" int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_ms, double* pro_ms) {
+  if (!e || nsteps <= 0) return SOP_ERR_ARG;
+  CK(cudaSetDevice(e->cfg.device));
+  int rc = refresh_layout(e);
+  if (rc) return rc;
+  if (e->active.empty()) return SOP_ERR_STATE;
+  const int nrep = (int)e->active.size();
+  k_begin<<<(nrep + 127) / 128, 128, 0, e->stream>>>(e->A.rep, e->d_ids, nrep, nsteps);
+  e->launches++;
+  const int64_t iters = nsteps + 1;
+  std::vector<cudaEvent_t> ev(3 * iters);
+  for (auto& x : ev) CK(cudaEventCreate(&x));
+  for (int64_t s = 0; s < iters; s++) {
+    CK(cudaEventRecord(ev[3 * s], e->stream));
+    CK(launch_prologue(e->A, e->d_ids, nrep, e->max_n, 0, 0, e->pro_grid, e->stream));
+    CK(cudaEventRecord(ev[3 * s + 1], e->stream));
+    CK(launch_step(e->A, e->d_items, (int)e->items.size(), e->max_staged, e->cfg.lanes_per_bead,
+                   e->cfg.block_threads, e->step_grid, e->stream));
+    CK(cudaEventRecord(ev[3 * s + 2], e->stream));
+    e->launches += 2;
+  }
+  CK(cudaStreamSynchronize(e->stream));
+  double ts = 0, tp = 0;
+  for (int64_t s = 0; s < iters; s++) {
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, ev[3 * s], ev[3 * s + 1]);
+    cudaEventElapsedTime(&b, ev[3 * s + 1], ev[3 * s + 2]);
+    tp += a;
+    ts += b;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (step_ms) *step_ms = ts / iters;
+  if (pro_ms) *pro_ms = tp / iters;
+  return check_errors(e);
+}
+
+extern "C" int sop_run_host(sop_engine* e, const double* xyz_in, const double* vel_in,
+                            int64_t nsteps, double* xyz_out, double* vel_out) {
+  if (!e || !xyz_in || nsteps < 0) return SOP_ERR_ARG;
+  int rc = refresh_layout(e);
+  if (rc) return rc;
+  std::vector<int> ids;
+  for (int r = 0; r < (int)e->reps.size(); r++)
+    if (e->reps[r].live) ids.push_back(r);
+  long long o = 0;
+  for (int r : ids) {
+    rc = upload_positions(e, r, xyz_in + o, 3);
+    if (rc) return rc;
+    rc = upload_velocities(e, r, vel_in ? vel_in + o : nullptr);
+    if (rc) return rc;
+    o += 3LL * e->reps[r].n;
+  }
+  rc = run_batched(e, nsteps, false);
+  if (rc) return rc;
+  o = 0;
+  for (int r : ids) {
+    rc = sop_replica_get_state(e, r, nullptr, xyz_out ? xyz_out + o : nullptr,
+                               vel_out ? vel_out + o : nullptr);
+    if (rc) return rc;
+    o += 3LL * e->reps[r].n;
+  }
+  return SOP_OK;
+}
+
+// ---- reference-named operations -------------------------------------------------
+
+extern "C" int sop_update_neighbor_list(sop_engine* e, int r) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  return build_now(e, r, SOP_LIST_NEIGHBOR);
+}
+
+extern "C" int sop_update_cell_list(sop_engine* e, int r) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  return build_now(e, r, SOP_LIST_CELL);
+}
+
+extern "C" int sop_update_pair_list(sop_engine* e, int r) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  Replica& R = e->reps[r];
+  CK(launch_pairlist(e->A, r, (int)R.off, R.n, e->stream));
+  e->launches++;
+  CK(cudaStreamSynchronize(e->stream));
+  return SOP_OK;
+}
+
+extern "C" int sop_get_pair_list(sop_engine* e, int r, int which, int* ii, int* jj, int cap,
+                                 int* count) {
+  if (!e || !live(e, r) || which < 0 || which > 3 || !count) return SOP_ERR_ARG;
+  Replica& R = e->reps[r];
+  CK(cudaMemsetAsync(e->A.pairs_cnt, 0, sizeof(int), e->stream));
+  CK(launch_export(e->A, r, (int)R.off, R.n, which, e->pairs_cap, e->stream));
+  e->launches++;
+  int n = 0;
+  CK(cudaMemcpyAsync(&n, e->A.pairs_cnt, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  if (n > e->pairs_cap) return SOP_ERR_OVERFLOW;
+  std::vector<unsigned long long> buf(n);
+  if (n) CK(cudaMemcpy(buf.data(), e->A.pairs_out, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  std::sort(buf.begin(), buf.end());
+  *count = n;
+  if (ii && jj) {
+    for (int k = 0; k < n && k < cap; k++) {
+      ii[k] = (int)(buf[k] >> 32);
+      jj[k] = (int)(buf[k] & 0xffffffffu);
+    }
+    if (n > cap) return SOP_ERR_OVERFLOW;
+  }
+  return SOP_OK;
+}
+
+static int run_phase(sop_engine* e, int r, int phase) {
+  Replica& R = e->reps[r];
+  std::vector<StepItem> items;
+  const int staged = R.n <= kStageMax;
+  for (int b = 0; b < R.n; b += e->chunk_beads) items.push_back(StepItem{r, b, std::min(R.n, b + e->chunk_beads), staged});
+  const long long item_slot = e->items_cap - (long long)items.size();
+  CK(h2d(e->d_items + item_slot, items.data(), items.size(), e->stream));
+  k_set_phase<<<1, 1, 0, e->stream>>>(e->A.rep, r, phase);
+  CK(launch_step(e->A, e->d_items + item_slot, (int)items.size(), staged ? R.n : 0,
+                 e->cfg.lanes_per_bead, e->cfg.block_threads,
+                 std::min((int)items.size(), 4 * e->prop.multiProcessorCount), e->stream));
+  e->launches += 2;
+  CK(cudaStreamSynchronize(e->stream));
+  return check_errors(e);
+}
+
+extern "C" int sop_force_eval(sop_engine* e, int r, double* force_xyz) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  int rc = run_phase(e, r, PH_FORCE);
+  if (rc) return rc;
+  Replica& R = e->reps[r];
+  if (force_xyz) {
+    const int n = R.n;
+    std::vector<double> soa(3 * (size_t)n);
+    for (int c = 0; c < 3; c++)
+      CK(cudaMemcpyAsync(soa.data() + (size_t)c * n, e->A.force + c * e->cap + R.off,
+                         n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    for (int i = 0; i < n; i++)
+      for (int c = 0; c < 3; c++) force_xyz[3 * i + c] = soa[(size_t)c * n + i];
+  }
+  return SOP_OK;
+}
+
+extern "C" int sop_energy_eval(sop_engine* e, int r, double* out) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  CK(cudaMemcpyAsync(e->d_ids + scratch_id(e, 0), &r, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  CK(launch_energy(e->A, e->d_ids + scratch_id(e, 0), 1, e->stream));
+  e->launches++;
+  RepDev d;
+  int rc = get_rep(e, r, &d);
+  if (rc) return rc;
+  if (out) std::memcpy(out, d.energy, sizeof d.energy);
+  return SOP_OK;
+}
+
+extern "C" int sop_observables(sop_engine* e, int r, double* out) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  CK(cudaMemcpyAsync(e->d_ids + scratch_id(e, 0), &r, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  CK(launch_observables(e->A, e->d_ids + scratch_id(e, 0), 1, e->stream));
+  e->launches++;
+  RepDev d;
+  int rc = get_rep(e, r, &d);
+  if (rc) return rc;
+  if (out) std::memcpy(out, d.obs, sizeof d.obs);
+  return SOP_OK;
+}
+
+extern "C" int sop_underdamped_iteration(sop_engine* e, int r) {
+  // incr = a1 v + a2 F, x += incr, F = force(x), v = a3 incr + a4 F: a run of one
+  // iteration (the restart step recomputes F at x with the same noise index)
+  return sop_run_plain(e, r, 1);
+}
+
+// ---- host-side numerics self-checks ------------------------------------------------
+
+extern "C" void sop_selftest_split(double x, float* hi, float* lo) {
+  float h, l;
+  split_double(x, h, l);
+  if (hi) *hi = h;
+  if (lo) *lo = l;
+}
+
+extern "C" void sop_selftest_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  philox4x32_10(ctr, key, out);
+}

@@ -1,0 +1,93 @@
+// Internal host-side state of the GB300 SOP engine (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <vector>
+
+#include "../../include/sop_gpu.h"
+#include "kernels.cuh"
+#include "sop_common.cuh"
+
+namespace sop {
+
+// First-fit allocator of index ranges inside one preallocated device array.
+class RangeAlloc {
+ public:
+  void init(long long cap) {
+    free_.clear();
+    if (cap > 0) free_[0] = cap;
+    cap_ = cap;
+    used_ = 0;
+  }
+  bool alloc(long long n, long long align, long long* out);
+  void release(long long start, long long n);
+  long long largest() const;
+  long long used() const { return used_; }
+  long long capacity() const { return cap_; }
+
+ private:
+  std::map<long long, long long> free_;
+  long long cap_ = 0, used_ = 0;
+};
+
+// Host record of one admitted system.
+struct Replica {
+  bool live = false;
+  int n = 0;
+  long long off = 0, nl_base = 0;
+  int L = 0;
+  long long nat_base = 0, nnat_e = 0, bnd_base = 0, nbnd_e = 0, ang_base = 0, nang_e = 0,
+            exc_base = 0, nexc_e = 0;
+  int nnat_pairs = 0;
+  sop_params params{};
+  std::vector<int> type, chain;
+};
+
+const FFTables& tables();
+
+}  // namespace sop
+
+struct sop_engine {
+  sop_engine_config cfg{};
+  cudaDeviceProp prop{};
+  cudaStream_t stream = nullptr;
+  sop::DevArrays A{};
+  long long cap = 0;
+  sop::RangeAlloc beads, lists, nats, bnds, angs, excs;
+  std::vector<sop::Replica> reps;
+  sop::RepDev* h_rep = nullptr;  // pinned staging for descriptor copies
+  // batched layout
+  int* d_ids = nullptr;             // active replica ids; scratch slots at the end
+  sop::StepItem* d_items = nullptr; // step work items; scratch at the end
+  long long items_cap = 0;
+  std::vector<int> active;
+  std::vector<sop::StepItem> items;
+  int max_n = 0, max_staged = 0, step_grid = 1, pro_grid = 1;
+  int chunk_beads = 256;
+  bool layout_dirty = true;
+  // CUDA graph of graph_steps batched steps
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_valid = false;
+  // bookkeeping
+  int pairs_cap = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int64_t launches = 0;
+  double last_total_ms = 0, last_step_ms = -1;
+  int64_t last_step_launches = 0;
+};
+
+namespace sop {
+int upload_positions(sop_engine* e, int r, const double* xyz, int which_bufs);
+int upload_velocities(sop_engine* e, int r, const double* vel);
+int get_rep(sop_engine* e, int r, RepDev* out);
+int put_rep(sop_engine* e, int r, const RepDev& d);
+int build_now(sop_engine* e, int r, int mode);
+int refresh_layout(sop_engine* e);
+int enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items, int nitems,
+                 int max_n, int max_staged, int step_grid, int pro_grid);
+int run_batched(sop_engine* e, int64_t nsteps, bool timed);
+inline int scratch_id(const sop_engine* e, int k) { return e->cfg.max_replicas + k; }
+}  // namespace sop

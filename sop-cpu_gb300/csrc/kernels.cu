@@ -1,0 +1,1130 @@
+// GB300 kernels of the SOP hot path.
+//
+//   k_prologue  per-replica step bookkeeping (phase, noise counter, the
+//               reference's nnlup cadence) and, when due, the list build:
+//               K1 cell binning (warp-match counting sort, stable by bead) and
+//               K2 neighbor/pair-list build over the 27-cell stencil, cutoffs
+//               decided bit-exactly against the reference's FP64 arithmetic.
+//   k_step      K3+K4 fused: pair/bond/angle forces in FP32 from positions
+//               staged in shared memory by TMA bulk copies, lane partials to
+//               int64 fixed point and reduced with warp shuffles, counter-
+//               based Langevin noise drawn in-kernel, the underdamped update
+//               with FP64 position accumulation, next step's pair-list bits.
+//   k_energy    K5 energy terms in FP64 with a fixed-order reduction.
+//   k_obs       K6 observables (Q, Rg^2, kinT) in FP64.
+//   k_pairlist  update_pair_list at the current positions.
+//   k_export    pair lists as (i<j) pairs for checking.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/sop_gpu.h"
+#include "kernels.cuh"
+#include "sop_common.cuh"
+
+namespace sop {
+
+__constant__ FFTables c_ff;
+
+void upload_tables(const FFTables& t, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_ff, &t, sizeof(FFTables), 0, cudaMemcpyHostToDevice, s);
+}
+
+// ---------------------------------------------------------------------------------
+// small helpers
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// d^2 - r0^2 between two staged beads, in two-float arithmetic (Knuth's
+// TwoSum, Dekker's exact product via FMA), accurate to ~2^-46 of d^2; also
+// returns dx (float, i -> j) and d^2 (float).  r0^2 = r0h + r0l.
+__device__ __forceinline__ float d2_minus(const float4& hi, const float4& lo, const float4& hj,
+                                          const float4& lj, float r0h, float r0l, float& dx,
+                                          float& dy, float& dz, float& d2) {
+  float sx, ex, sy, ey, sz, ez;
+  two_sum(hj.x, -hi.x, sx, ex);
+  two_sum(hj.y, -hi.y, sy, ey);
+  two_sum(hj.z, -hi.z, sz, ez);
+  const float tx = ex + (lj.x - lo.x), ty = ey + (lj.y - lo.y), tz = ez + (lj.z - lo.z);
+  const float px = sx * sx, py = sy * sy, pz = sz * sz;
+  const float pex = fmaf(sx, sx, -px), pey = fmaf(sy, sy, -py), pez = fmaf(sz, sz, -pz);
+  float a, ea, bb, eb, c, ec;
+  two_sum(px, py, a, ea);
+  two_sum(a, pz, bb, eb);
+  two_sum(bb, -r0h, c, ec);
+  const float tail = ea + eb + ec + pex + pey + pez + 2.0f * (sx * tx + sy * ty + sz * tz) - r0l;
+  dx = sx + tx;
+  dy = sy + ty;
+  dz = sz + tz;
+  d2 = bb;
+  return c + tail;
+}
+
+// FP64 squared distance with the reference's operation order and no FMA
+// (neighbor_list.cpp:27-37, sop.cpp:496-507).  Callers guarantee the minimum
+// image is the identity (extent checked at every build), as rnd(dx/boxl) = 0.
+__device__ __forceinline__ double exact_d2(const double* X, long long cap, long long gi,
+                                           long long gj) {
+  double dx = __dsub_rn(X[gj], X[gi]);
+  double dy = __dsub_rn(X[cap + gj], X[cap + gi]);
+  double dz = __dsub_rn(X[2 * cap + gj], X[2 * cap + gi]);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// d2 < rc2, screened in FP32 and re-decided in FP64 inside a relative band.
+template <class Exact>
+__device__ __forceinline__ bool within(float d2, float rc2f, float margin, Exact exact) {
+  if (d2 < rc2f * (1.0f - margin)) return true;
+  if (d2 > rc2f * (1.0f + margin)) return false;
+  return exact();
+}
+
+__device__ __forceinline__ void bead_normals(unsigned seed_lo, unsigned seed_hi,
+                                             long long t, int bead, float n[3]) {
+  uint32_t ctr[4] = {(uint32_t)bead, (uint32_t)t, (uint32_t)((unsigned long long)t >> 32), 0u};
+  uint32_t key[2] = {seed_lo, seed_hi};
+  uint32_t o[4];
+  philox4x32_10(ctr, key, o);
+  const float k32 = 2.3283064365386963e-10f, k33 = 1.1641532182693481e-10f;
+  float u0 = fmaf(__uint2float_rn(o[0]), k32, k33);
+  float u1 = fmaf(__uint2float_rn(o[1]), k32, k33);
+  float u2 = fmaf(__uint2float_rn(o[2]), k32, k33);
+  float u3 = fmaf(__uint2float_rn(o[3]), k32, k33);
+  float r0 = sqrtf(-2.0f * logf(u0));
+  float r1 = sqrtf(-2.0f * logf(u2));
+  float s0, c0, s1, c1;
+  sincospif(2.0f * u1, &s0, &c0);
+  sincospif(2.0f * u3, &s1, &c1);
+  n[0] = r0 * c0;
+  n[1] = r0 * s0;
+  n[2] = r1 * c1;
+}
+
+__device__ __forceinline__ bool finite3(float a, float b, float c) {
+  return isfinite(a) && isfinite(b) && isfinite(c);
+}
+
+// ---- mbarrier + TMA bulk copy (cp.async.bulk) ------------------------------------
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                             unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------------
+// K1 + K2: list build of one replica by one CTA (n <= kBuildMax)
+
+struct BuildSmem {
+  int cstart[kMaxCells + 1];
+  int ccur[kMaxCells];
+  float red[6][32];
+  int s_ok, s_nx, s_ny, s_nz, s_maxrow, s_status;
+  float s_edge, s_ox, s_oy, s_oz;
+  int s_cx0, s_cy0, s_cz0;
+};
+
+__device__ __forceinline__ int bsearch_sorted(const int* a, int n, int key) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    int v = a[mid];
+    if (v == key) return mid;
+    if (v < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return -1;
+}
+
+// Build the replica's lists from position buffer `src` in list mode `mode`.
+// Dynamic shared memory: float4 P[n] | int sorted[n] | ushort cell[n].
+__device__ void build_lists(const DevArrays& A, int r, int src, int mode, BuildSmem& B,
+                            unsigned char* dyn) {
+  RepDev* R = &A.rep[r];
+  const int n = R->n, off = R->off, tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  float4* P = reinterpret_cast<float4*>(dyn);
+  int* sorted = reinterpret_cast<int*>(P + n);
+  unsigned short* cell = reinterpret_cast<unsigned short*>(sorted + n);
+  const float4* S = A.stage[src] + 2 * (long long)off;
+  const double* X = A.X[src];
+  const long long cap = A.cap;
+  const double boxl = R->boxl;
+  const float skin = R->skin;
+
+  // list cutoff per type pair (non-natives) and the largest one
+  float rl_max = 0.f;
+  for (int a = 1; a < kMaxTypes; a++)
+    for (int b = 1; b < kMaxTypes; b++) {
+      float rl = (mode == SOP_LIST_SKIN) ? (float)(2.5 * c_ff.sigma_rep[a][b]) + skin
+                                         : (float)(3.2 * c_ff.sigma_rep[a][b]);
+      rl_max = fmaxf(rl_max, rl);
+    }
+
+  // 1. bounding box of hi positions
+  float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+  for (int i = tid; i < n; i += nt) {
+    float4 h = S[2 * i];
+    mn[0] = fminf(mn[0], h.x); mn[1] = fminf(mn[1], h.y); mn[2] = fminf(mn[2], h.z);
+    mx[0] = fmaxf(mx[0], h.x); mx[1] = fmaxf(mx[1], h.y); mx[2] = fmaxf(mx[2], h.z);
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int c = 0; c < 3; c++) {
+      mn[c] = fminf(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
+      mx[c] = fmaxf(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
+    }
+  if (lane == 0)
+    for (int c = 0; c < 3; c++) { B.red[c][warp] = mn[c]; B.red[3 + c][warp] = mx[c]; }
+  __syncthreads();
+  if (tid == 0) {
+    float m0[3] = {3.4e38f, 3.4e38f, 3.4e38f}, m1[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (int w = 0; w < nwarp; w++)
+      for (int c = 0; c < 3; c++) {
+        m0[c] = fminf(m0[c], B.red[c][w]);
+        m1[c] = fmaxf(m1[c], B.red[3 + c][w]);
+      }
+    int status = 0;
+    float ext = fmaxf(m1[0] - m0[0], fmaxf(m1[1] - m0[1], m1[2] - m0[2]));
+    bool finite_box = true;
+    for (int c = 0; c < 3; c++)
+      finite_box = finite_box && isfinite(m0[c]) && isfinite(m1[c]) && m1[c] >= m0[c] &&
+                   fabsf(m0[c]) < 1e6f && fabsf(m1[c]) < 1e6f;
+    if (!finite_box) {  // non-finite or runaway positions: no grid can be built
+      B.s_status = SOP_ST_NONFINITE;
+      B.s_ok = 0;
+    } else {
+    // the minimum image must be the identity for every candidate pair
+    if ((double)ext + 2.0 * rl_max >= 0.5 * boxl) status |= SOP_ST_PERIODIC;
+    int nx, ny, nz;
+    float edge;
+    if (mode == SOP_LIST_CELL) {
+      // reference cells floor(x / lcell) (cell_list.cpp:24-31), FP64
+      double lc = R->lcell;
+      int c0[3], c1[3];
+      for (int c = 0; c < 3; c++) {
+        c0[c] = (int)floor(__ddiv_rn((double)m0[c] - 1e-3 * fabs((double)m0[c]) - 1e-3, lc));
+        c1[c] = (int)floor(__ddiv_rn((double)m1[c] + 1e-3 * fabs((double)m1[c]) + 1e-3, lc));
+      }
+      B.s_cx0 = c0[0]; B.s_cy0 = c0[1]; B.s_cz0 = c0[2];
+      nx = c1[0] - c0[0] + 1; ny = c1[1] - c0[1] + 1; nz = c1[2] - c0[2] + 1;
+      if (2.0 * (double)(max(nx, max(ny, nz)) + 1) >= R->ncell) status |= SOP_ST_PERIODIC;
+      edge = (float)lc;
+      if ((long long)nx * ny * nz > kMaxCells) status |= SOP_ST_GRID;
+    } else {
+      edge = (mode == SOP_LIST_NONE) ? 3.0e38f : fmaxf(R->cell_edge, rl_max * 1.0001f + 1e-3f);
+      for (;;) {
+        nx = (mode == SOP_LIST_NONE) ? 1 : (int)((m1[0] - m0[0]) / edge) + 1;
+        ny = (mode == SOP_LIST_NONE) ? 1 : (int)((m1[1] - m0[1]) / edge) + 1;
+        nz = (mode == SOP_LIST_NONE) ? 1 : (int)((m1[2] - m0[2]) / edge) + 1;
+        if ((long long)nx * ny * nz <= kMaxCells) break;
+        edge *= 1.25f;
+      }
+    }
+    B.s_status = status;
+    B.s_ok = !(status & SOP_ST_GRID) && nx >= 1 && ny >= 1 && nz >= 1;
+    B.s_nx = nx; B.s_ny = ny; B.s_nz = nz;
+    B.s_edge = edge;
+    B.s_ox = m0[0]; B.s_oy = m0[1]; B.s_oz = m0[2];
+    B.s_maxrow = 0;
+    }
+  }
+  __syncthreads();
+  if (!B.s_ok) {
+    if (tid == 0) atomicOr(&R->status, B.s_status);
+    return;
+  }
+  const int nx = B.s_nx, ny = B.s_ny, nz = B.s_nz, ncell = nx * ny * nz;
+  const float edge = B.s_edge, ox = B.s_ox, oy = B.s_oy, oz = B.s_oz;
+
+  // 2. relative positions (hi - origin) + lo, type|chain code, cell index
+  for (int i = tid; i < n; i += nt) {
+    float4 h = S[2 * i], l = S[2 * i + 1];
+    float4 p;
+    p.x = (h.x - ox) + l.x;
+    p.y = (h.y - oy) + l.y;
+    p.z = (h.z - oz) + l.z;
+    p.w = h.w + 4.0f * l.w;  // type + 4 * chain (exact below 2^22 chains)
+    P[i] = p;
+    int cx, cy, cz;
+    if (mode == SOP_LIST_CELL) {
+      double lc = R->lcell;
+      cx = (int)floor(__ddiv_rn(X[off + i], lc)) - B.s_cx0;
+      cy = (int)floor(__ddiv_rn(X[cap + off + i], lc)) - B.s_cy0;
+      cz = (int)floor(__ddiv_rn(X[2 * cap + off + i], lc)) - B.s_cz0;
+      cx = min(max(cx, 0), nx - 1); cy = min(max(cy, 0), ny - 1); cz = min(max(cz, 0), nz - 1);
+    } else if (mode == SOP_LIST_NONE) {
+      cx = cy = cz = 0;
+    } else {
+      cx = min(max((int)(p.x / edge), 0), nx - 1);
+      cy = min(max((int)(p.y / edge), 0), ny - 1);
+      cz = min(max((int)(p.z / edge), 0), nz - 1);
+    }
+    cell[i] = (unsigned short)(cx + nx * (cy + ny * cz));
+  }
+  for (int c = tid; c < ncell; c += nt) B.ccur[c] = 0;
+  __syncthreads();
+
+  // 3. counting sort: per-cell counts, warp-aggregated through __match_any_sync
+  for (int base = 0; base < n; base += nt) {
+    int i = base + tid;
+    bool valid = i < n;
+    unsigned act = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
+      int c = cell[i];
+      unsigned m = __match_any_sync(act, c);
+      if (lane == __ffs(m) - 1) atomicAdd(&B.ccur[c], __popc(m));
+    }
+  }
+  __syncthreads();
+  // exclusive scan of counts (one warp, ncell <= kMaxCells)
+  if (warp == 0) {
+    int carry = 0;
+    for (int base = 0; base < ncell; base += 32) {
+      int c = base + lane;
+      int v = c < ncell ? B.ccur[c] : 0;
+      int x = v;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (c < ncell) B.cstart[c] = carry + x - v;
+      carry += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (lane == 0) B.cstart[ncell] = carry;
+  }
+  __syncthreads();
+  for (int c = tid; c < ncell; c += nt) B.ccur[c] = 0;
+  __syncthreads();
+  // stable scatter in bead order (warp 0, 32 beads at a time)
+  if (warp == 0) {
+    for (int base = 0; base < n; base += 32) {
+      int i = base + lane;
+      bool valid = i < n;
+      unsigned act = __ballot_sync(0xffffffffu, valid);
+      int c = valid ? cell[i] : -1;
+      unsigned m = valid ? __match_any_sync(act, c) : 0u;
+      int rank = __popc(m & ((1u << lane) - 1u));
+      int basec = valid ? B.ccur[c] : 0;
+      __syncwarp();
+      if (valid) sorted[B.cstart[c] + basec + rank] = i;
+      if (valid && lane == __ffs(m) - 1) B.ccur[c] = basec + __popc(m);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+
+  // 4. neighbor enumeration: one thread per bead, stencil in fixed order
+  const long long nl_base = R->nl_base;
+  const int L = R->L;
+  const float margin = 1e-5f;
+  int my_status = 0, my_max = 0;
+  for (int i = tid; i < n; i += nt) {
+    const float4 pi = P[i];
+    const int code_i = (int)pi.w, ti = code_i & 3, chi = code_i >> 2;
+    const int c = cell[i];
+    const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
+    const int4 tp = A.topo[off + i];
+    const int nat_cnt = tp.w & 0xFFFF;
+    const int2 er = A.exc_rng[off + i];
+    const long long row = nl_base + (long long)i * L;
+    const long long gi = off + i;
+    // list cutoff^2 against partner type 1 and 2 (neighbor_list.cpp:97-100, or 2.5 sigma + skin)
+    double rl2d[kMaxTypes];
+    float rl2f[kMaxTypes];
+    for (int t = 1; t < kMaxTypes; t++) {
+      double rl = 2.5 * c_ff.sigma_rep[ti][t] + (double)skin;
+      rl2d[t] = (mode == SOP_LIST_SKIN) ? rl * rl : c_ff.rc2_nl[ti][t];
+      rl2f[t] = (float)rl2d[t];
+    }
+    rl2d[0] = rl2d[1];
+    rl2f[0] = rl2f[1];
+    int cnt = 0;
+    for (int dz = -1; dz <= 1; dz++) {
+      int zz = cz + dz;
+      if (zz < 0 || zz >= nz) continue;
+      for (int dy = -1; dy <= 1; dy++) {
+        int yy = cy + dy;
+        if (yy < 0 || yy >= ny) continue;
+        for (int dx = -1; dx <= 1; dx++) {
+          int xx = cx + dx;
+          if (xx < 0 || xx >= nx) continue;
+          int cc = xx + nx * (yy + ny * zz);
+          for (int s = B.cstart[cc], e = B.cstart[cc + 1]; s < e; s++) {
+            int j = sorted[s];
+            if (j == i) continue;
+            float4 pj = P[j];
+            int code_j = (int)pj.w, tj = code_j & 3, chj = code_j >> 2;
+            if (chi == chj && abs(i - j) <= 2) continue;
+            float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
+            float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            const long long gj = off + j;
+            bool inl, inp;
+            if (mode == SOP_LIST_NONE || mode == SOP_LIST_CELL) {
+              inl = true;  // cell adjacency is the whole predicate (cell_list.cpp:86-88)
+            } else {
+              // cheap rejection first: most stencil candidates lie outside the list sphere
+              if (d2 > rl2f[tj] * (1.0f + margin)) continue;
+              const double rl2 = rl2d[tj];
+              inl = within(d2, (float)rl2, margin, [&] { return exact_d2(X, cap, gi, gj) < rl2; });
+            }
+            if (!inl) continue;
+            // natives are listed separately (sorted by partner)
+            bool is_nat = false;
+            {
+              int lo = 0, hi = nat_cnt;
+              while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                int v = A.nat[tp.x + mid].x & (int)kIdx;
+                if (v == j) { is_nat = true; break; }
+                if (v < j) lo = mid + 1;
+                else hi = mid;
+              }
+            }
+            if (is_nat) continue;
+            if (er.y > 0 && bsearch_sorted(A.exc + er.x, er.y, j) >= 0) continue;
+            if (mode == SOP_LIST_NONE) {
+              inp = true;  // no pair-list filter without a cutoff type
+            } else {
+              double rc2 = c_ff.rc2_pl[ti][tj];
+              inp = within(d2, (float)rc2, margin, [&] { return exact_d2(X, cap, gi, gj) < rc2; });
+            }
+            if (cnt < L) A.nl[row + cnt] = j | (inp ? (int)kPL : 0);
+            cnt++;
+          }
+        }
+      }
+    }
+    if (cnt > L) my_status |= SOP_ST_LIST_OVERFLOW;
+    my_max = max(my_max, cnt);
+    A.nl_cnt[off + i] = min(cnt, L);
+    // natives: neighbor-list and pair-list bits
+    for (int k = 0; k < nat_cnt; k++) {
+      int4 e = A.nat[tp.x + k];
+      int j = e.x & (int)kIdx;
+      float4 pj = P[j];
+      float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
+      float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+      double r0 = A.nat_r0[tp.x + k];
+      const long long gj = off + j;
+      bool nlb, plb;
+      if (mode == SOP_LIST_NEIGHBOR) {
+        double rc = 3.2 * r0, rc2 = rc * rc;  // neighbor_list.cpp:44-47
+        nlb = within(d2, (float)rc2, margin, [&] { return exact_d2(X, cap, gi, gj) < rc2; });
+      } else if (mode == SOP_LIST_CELL) {
+        int c2 = cell[j];
+        int jx = c2 % nx, jy = (c2 / nx) % ny, jz = c2 / (nx * ny);
+        nlb = abs(jx - cx) <= 1 && abs(jy - cy) <= 1 && abs(jz - cz) <= 1;
+      } else {
+        nlb = true;
+      }
+      if (mode == SOP_LIST_NONE) {
+        plb = true;
+      } else if (nlb) {
+        double rc = 2.5 * r0, rc2 = rc * rc;  // sop.cpp:504-506
+        plb = within(d2, (float)rc2, margin, [&] { return exact_d2(X, cap, gi, gj) < rc2; });
+      } else {
+        plb = false;
+      }
+      A.nat[tp.x + k].x = j | (nlb ? (int)kNL : 0) | (plb ? (int)kPL : 0);
+    }
+    float4 h = S[2 * i];
+    A.xb[off + i] = make_float4(h.x, h.y, h.z, 0.f);
+  }
+  atomicMax(&B.s_maxrow, my_max);
+  if (my_status) atomicOr(&B.s_status, my_status);
+  __syncthreads();
+  if (tid == 0) {
+    R->max_row = B.s_maxrow;
+    R->builds += 1;
+    R->rebuild = 0;
+    if (B.s_status) atomicOr(&R->status, B.s_status);
+  }
+}
+
+__device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* red);
+__device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red);
+
+// Per-replica step bookkeeping.  CTA b handles replica ids b, b+grid, ...:
+// one thread per replica first decides the step (phase, noise counter, the
+// reference's nnlup cadence or the displacement trigger, output), then the
+// CTA does that replica's due work in order:
+//   observables of the previous output step (positions X_{t-1}, velocities v_{t-1}),
+//   the list build from X_{t-1} (sop.cpp:156-170: rebuild before the step),
+//   the energies of this output step at X_t with pair list PL_t.
+// Energies must precede the step kernel, which rewrites the pair-list bits.
+__global__ void __launch_bounds__(kBuildThreads, 1) k_prologue(DevArrays A, const int* rep_ids,
+                                                            int nrep, int force_build,
+                                                            int build_mode) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  __shared__ BuildSmem B;
+  __shared__ int s_obs[64], s_build[64], s_en[64], s_prev[64], s_cur[64], s_mode[64];
+  double* red = reinterpret_cast<double*>(dyn);
+  const int per = (nrep + gridDim.x - 1) / gridDim.x;
+  for (int chunk = 0; chunk < per; chunk += 64) {
+    const int tid = threadIdx.x;
+    if (tid < 64) {
+      s_obs[tid] = s_build[tid] = s_en[tid] = 0;
+      int k = blockIdx.x + (chunk + tid) * gridDim.x;
+      if (chunk + tid < per && k < nrep) {
+        RepDev* R = &A.rep[rep_ids[k]];
+        s_prev[tid] = s_cur[tid] = R->cur;
+        s_mode[tid] = R->mode;
+        if (force_build) {
+          s_build[tid] = 1;
+          s_mode[tid] = build_mode;
+        } else {
+          if (R->obs_pending) { s_obs[tid] = 1; R->obs_pending = 0; }
+          if (!R->active || !R->running ||
+              (R->status & (SOP_ST_NONFINITE | SOP_ST_LIST_OVERFLOW | SOP_ST_PERIODIC | SOP_ST_GRID))) {
+            R->phase = PH_SKIP;
+            R->out = 0;
+          } else {
+            if (R->moved) {
+              bool need = false;
+              if (R->mode == SOP_LIST_NEIGHBOR || R->mode == SOP_LIST_CELL) {
+                // underdamped_ctrl cadence (sop.cpp:156-165), local inlup from 1
+                if (R->inlup % R->nnlup == 0) { need = true; R->inlup = 0; }
+                R->inlup++;
+              } else if (R->mode == SOP_LIST_SKIN) {
+                need = R->rebuild != 0;
+              }
+              s_build[tid] = need;
+              R->cur ^= 1;
+              R->moved = 0;
+            }
+            int ph;
+            if (R->first_pending) { ph = PH_FIRST; R->first_pending = 0; }
+            else if (R->t >= R->t_end) ph = PH_FINAL;
+            else ph = PH_NORMAL;
+            R->t_cur = R->t;
+            if (ph == PH_FINAL) {
+              R->running = 0;
+            } else {
+              R->t += 1;
+              R->moved = 1;
+            }
+            R->phase = ph;
+            R->out = (ph == PH_NORMAL || ph == PH_FINAL) && R->nup > 0 && R->t_cur > 0 &&
+                     (R->t_cur % R->nup) == 0;
+            if (R->out) { s_en[tid] = 1; R->obs_pending = 1; }
+            s_cur[tid] = R->cur;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    for (int q = 0; q < 64 && chunk + q < per; q++) {
+      if (!(s_obs[q] | s_build[q] | s_en[q])) continue;
+      const int k = blockIdx.x + (chunk + q) * gridDim.x;
+      RepDev* R = &A.rep[rep_ids[k]];
+      if (s_obs[q]) replica_obs(A, R, s_prev[q], red);
+      if (s_build[q]) { build_lists(A, rep_ids[k], s_prev[q], s_mode[q], B, dyn); __syncthreads(); }
+      if (s_en[q]) replica_energy(A, R, s_cur[q], red);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// K3 + K4: fused force + underdamped step
+
+struct ItemCtx {
+  int r, off, n, cur, phase, terms, mode, out, ti_dummy;
+  long long nl_base, t_cur;
+  int L;
+  float a1, a2, a3, a4, amp, T, kbnd, R0sq, fang, half_skin2, pull_f;
+  int pull_i, pull_j;
+  unsigned seed_lo, seed_hi;
+};
+
+template <bool ST>
+__device__ __forceinline__ float4 ldp(const float4* S, int k) {
+  if (ST) return S[k];
+  return __ldg(S + k);
+}
+
+template <int G, bool ST>
+__device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, const float4* S,
+                                          int i, int lane, unsigned gmask) {
+  const long long g = (long long)C.off + i;
+  const long long cap = A.cap;
+  const float4 hi = ldp<ST>(S, 2 * i), lo = ldp<ST>(S, 2 * i + 1);
+  const int ti = (int)hi.w;
+  const int4 tp = A.topo[g];
+  const int nat_cnt = tp.w & 0xFFFF, bnd_cnt = (tp.w >> 16) & 0xFF, ang_cnt = (tp.w >> 24) & 0xFF;
+  const bool upd = (C.phase == PH_FIRST || C.phase == PH_NORMAL) && C.mode != SOP_LIST_NONE;
+  const double* Xc = A.X[C.cur];
+  const float margin = kScreenMargin;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  int st = 0;
+
+  if (C.terms & SOP_TERM_VDW) {
+    // native 12-6 attraction (energy.cpp:274-311).  The force vanishes at the
+    // native distance, so (r0/d)^12 - (r0/d)^6 is formed from r0^2 - d^2 in
+    // two-float arithmetic: with u = r0^2/d^2 - 1, s^3 - 1 = u (u^2 + 3u + 3).
+    for (int k = lane; k < nat_cnt; k += G) {
+      const int4 e = A.nat[tp.x + k];
+      const int j = e.x & (int)kIdx;
+      const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
+      const float r0sq = __int_as_float(e.y);
+      float dx, dy, dz, d2;
+      const float diff = d2_minus(hi, lo, hj, lj, r0sq, __int_as_float(e.z), dx, dy, dz, d2);
+      if (e.x & (int)kPL) {
+        if (d2 >= (float)kTol * r0sq) {
+          const int tj = (int)hj.w;
+          const float inv = 1.0f / d2;
+          const float u = -diff * inv;                 // s - 1, s = r0^2/d^2
+          const float s3m1 = u * fmaf(u, u + 3.0f, 3.0f);  // s^3 - 1
+          const float s3 = 1.0f + s3m1;
+          const float co = c_ff.fca[ti][tj] * inv * (s3 * s3m1);
+          fx += co * dx; fy += co * dy; fz += co * dz;
+        }
+      }
+      if (upd) {
+        bool plb = false;
+        if (e.x & (int)kNL) {
+          plb = within(d2, 6.25f * r0sq, margin, [&] {
+            double rc = 2.5 * A.nat_r0[tp.x + k], rc2 = rc * rc;
+            return exact_d2(Xc, cap, g, (long long)C.off + j) < rc2;
+          });
+        }
+        if (plb != ((e.x & (int)kPL) != 0)) A.nat[tp.x + k].x = e.x ^ (int)kPL;
+      }
+    }
+    // non-native repulsion (energy.cpp:313-350)
+    const int cnt = A.nl_cnt[g];
+    const long long row = C.nl_base + (long long)i * C.L;
+    for (int k = lane; k < cnt; k += G) {
+      const int e = A.nl[row + k];
+      const int j = e & (int)kIdx;
+      const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
+      const float dx = (hj.x - hi.x) + (lj.x - lo.x);
+      const float dy = (hj.y - hi.y) + (lj.y - lo.y);
+      const float dz = (hj.z - hi.z) + (lj.z - lo.z);
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      const int tj = (int)hj.w;
+      const float s2 = c_ff.s2[ti][tj];
+      if (e & (int)kPL) {
+        if (d2 >= s2 * (float)kTol) {
+          const float inv = 1.0f / d2;
+          const float s = s2 * inv, s3 = s * s * s;
+          const float co = c_ff.fcr[ti][tj] * inv * (2.0f * s3 * s3 + s3);
+          fx += co * dx; fy += co * dy; fz += co * dz;
+        }
+      }
+      if (upd) {
+        const double rc2 = c_ff.rc2_pl[ti][tj];
+        const bool plb = within(d2, (float)rc2, margin, [&] {
+          return exact_d2(Xc, cap, g, (long long)C.off + j) < rc2;
+        });
+        if (plb != ((e & (int)kPL) != 0)) A.nl[row + k] = e ^ (int)kPL;
+      }
+    }
+  }
+  if (C.terms & SOP_TERM_FENE) {
+    // FENE (energy.cpp:402-447); d^2 - r0^2 in two-float arithmetic so the
+    // stretch dev = (d^2 - r0^2)/(d + r0) keeps FP32 relative accuracy.
+    for (int k = lane; k < bnd_cnt; k += G) {
+      const int4 b = A.bnd[tp.y + k];
+      const int j = b.x;
+      const float r0 = __int_as_float(b.y), r0h = __int_as_float(b.z), r0l = __int_as_float(b.w);
+      const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
+      float dx, dy, dz, d2;
+      const float diff = d2_minus(hi, lo, hj, lj, r0h, r0l, dx, dy, dz, d2);  // d^2 - r0^2
+      const float d = sqrtf(d2);
+      const float dev = diff / (d + r0);
+      const float den = 1.0f - dev * dev / C.R0sq;
+      if (!(den > 0.f)) st |= SOP_ST_FENE;
+      const float temp = -C.kbnd * dev / d / den;
+      fx -= temp * dx; fy -= temp * dy; fz -= temp * dz;
+    }
+  }
+  if (C.terms & SOP_TERM_ANGLE) {
+    // i,i+2 soft-sphere repulsion (energy.cpp:354-400)
+    for (int k = lane; k < ang_cnt; k += G) {
+      const int j = A.ang[tp.z + k];
+      const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
+      const float dx = (hj.x - hi.x) + (lj.x - lo.x);
+      const float dy = (hj.y - hi.y) + (lj.y - lo.y);
+      const float dz = (hj.z - hi.z) + (lj.z - lo.z);
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      const float d4 = d2 * d2, d8 = d4 * d4;
+      const float co = C.fang / d8;
+      fx -= co * dx; fy -= co * dy; fz -= co * dz;
+    }
+  }
+
+  // lane partials -> int64 fixed point -> exact cross-lane sum
+  long long Fx = fixed_from_float(fx), Fy = fixed_from_float(fy), Fz = fixed_from_float(fz);
+  if (!finite3(fx, fy, fz) || fabsf(fx) > kFixMax || fabsf(fy) > kFixMax || fabsf(fz) > kFixMax)
+    st |= SOP_ST_NONFINITE;
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    Fx += __shfl_xor_sync(gmask, Fx, o, G);
+    Fy += __shfl_xor_sync(gmask, Fy, o, G);
+    Fz += __shfl_xor_sync(gmask, Fz, o, G);
+  }
+  st |= __reduce_or_sync(gmask, st);
+  if (lane != 0) return;
+
+  float F[3] = {float_from_fixed(Fx), float_from_fixed(Fy), float_from_fixed(Fz)};
+  if ((C.terms & SOP_TERM_RANDOM) && C.amp > 0.f) {
+    float nrm[3];
+    bead_normals(C.seed_lo, C.seed_hi, C.t_cur, i, nrm);
+    F[0] += C.amp * nrm[0]; F[1] += C.amp * nrm[1]; F[2] += C.amp * nrm[2];
+  }
+  if (C.pull_f != 0.f && (i == C.pull_i || i == C.pull_j)) {
+    const int o = (i == C.pull_i) ? C.pull_j : C.pull_i;
+    const float4 ho = ldp<ST>(S, 2 * o), lo2 = ldp<ST>(S, 2 * o + 1);
+    float ux = (ho.x - hi.x) + (lo2.x - lo.x), uy = (ho.y - hi.y) + (lo2.y - lo.y),
+          uz = (ho.z - hi.z) + (lo2.z - lo.z);
+    float inv = rsqrtf(ux * ux + uy * uy + uz * uz);
+    F[0] -= C.pull_f * ux * inv; F[1] -= C.pull_f * uy * inv; F[2] -= C.pull_f * uz * inv;
+  }
+  if (C.phase == PH_FORCE || C.phase == PH_FINAL) {
+    for (int c = 0; c < 3; c++) A.force[c * cap + g] = f2d_exact(F[c]);
+  }
+  if (C.phase != PH_FORCE) {
+    const bool keepv = (C.phase == PH_FIRST) || (C.T < (float)kEpsT);
+    float v[3];
+    for (int c = 0; c < 3; c++) {
+      if (keepv) {
+        float h, l;
+        split_double(A.vel[c * cap + g], h, l);
+        v[c] = h;
+      } else {
+        v[c] = C.a3 * A.incr[c * cap + g] + C.a4 * F[c];
+      }
+    }
+    if (!keepv && (C.out || C.phase == PH_FINAL))
+      for (int c = 0; c < 3; c++) A.vel[c * cap + g] = f2d_exact(v[c]);
+    if (C.phase != PH_FINAL) {
+      const int nb = C.cur ^ 1;
+      float h[3], l[3];
+      double xn[3];
+      for (int c = 0; c < 3; c++) {
+        const float inc = C.a1 * v[c] + C.a2 * F[c];
+        xn[c] = Xc[c * cap + g] + f2d_exact(inc);  // the FP64 accumulation
+        A.X[nb][c * cap + g] = xn[c];
+        A.incr[c * cap + g] = inc;
+        split_double(xn[c], h[c], l[c]);
+      }
+      A.stage[nb][2 * g] = make_float4(h[0], h[1], h[2], hi.w);
+      A.stage[nb][2 * g + 1] = make_float4(l[0], l[1], l[2], lo.w);
+      if (C.mode == SOP_LIST_SKIN) {
+        const float4 b = A.xb[g];
+        const float ex = h[0] - b.x, ey = h[1] - b.y, ez = h[2] - b.z;
+        if (ex * ex + ey * ey + ez * ez > C.half_skin2) A.rep[C.r].rebuild = 1;
+      }
+      if (!(isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]))) st |= SOP_ST_NONFINITE;
+    }
+  }
+  if (!finite3(F[0], F[1], F[2])) st |= SOP_ST_NONFINITE;
+  if (st) atomicOr(&A.rep[C.r].status, st);
+}
+
+template <int G>
+__global__ void __launch_bounds__(256, 3) k_step(DevArrays A, const StepItem* items, int nitems) {
+  extern __shared__ __align__(128) float4 sst[];
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ ItemCtx sC;
+  const int lane = threadIdx.x & (G - 1);
+  const int grp = threadIdx.x / G, ngrp = blockDim.x / G;
+  const unsigned gmask =
+      (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+  if (threadIdx.x == 0) mbar_init(&mbar, 1);
+  fence_async_smem();
+  __syncthreads();
+  uint32_t parity = 0;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const StepItem w = items[it];
+    if (threadIdx.x == 0) {
+      const RepDev* R = &A.rep[w.r];
+      ItemCtx C;
+      C.r = w.r; C.off = R->off; C.n = R->n; C.cur = R->cur; C.phase = R->phase;
+      C.terms = R->terms; C.mode = R->mode; C.out = R->out;
+      C.nl_base = R->nl_base; C.t_cur = R->t_cur; C.L = R->L;
+      C.a1 = R->a1; C.a2 = R->a2; C.a3 = R->a3; C.a4 = R->a4;
+      C.amp = R->noise_amp; C.T = R->T; C.kbnd = R->kbnd; C.R0sq = R->R0sq; C.fang = R->fang;
+      C.half_skin2 = R->half_skin2; C.pull_f = R->pull_f; C.pull_i = R->pull_i;
+      C.pull_j = R->pull_j; C.seed_lo = R->seed_lo; C.seed_hi = R->seed_hi;
+      sC = C;
+      if (C.phase != PH_SKIP && w.staged) {
+        const char* src = reinterpret_cast<const char*>(A.stage[C.cur] + 2 * (long long)C.off);
+        const uint32_t bytes = (uint32_t)C.n * 32u;
+        fence_async_smem();
+        mbar_expect_tx(&mbar, bytes);
+        for (uint32_t o = 0; o < bytes; o += 32768u) {
+          const uint32_t b = (bytes - o < 32768u) ? bytes - o : 32768u;
+          tma_bulk_g2s(reinterpret_cast<char*>(sst) + o, src + o, b, &mbar);
+        }
+      }
+    }
+    __syncthreads();
+    const ItemCtx C = sC;
+    if (C.phase != PH_SKIP) {
+      if (w.staged) {
+        long long spins = 0;
+        while (!mbar_try_wait(&mbar, parity)) {
+          if (++spins > (1LL << 26)) {  // never expected: record and stop waiting
+            atomicOr(A.err, 1);
+            break;
+          }
+        }
+        parity ^= 1u;
+        for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, true>(A, C, sst, b, lane, gmask);
+      } else {
+        const float4* S = A.stage[C.cur] + 2 * (long long)C.off;
+        for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, false>(A, C, S, b, lane, gmask);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// K5: energies in FP64 (energy.cpp:115-257), deterministic fixed-order sums
+
+__device__ void block_sum(double* v, int nv, double* red) {
+  // red: [nv][blockDim], reduced in a fixed tree order
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int q = 0; q < nv; q++) red[q * nt + tid] = v[q];
+  __syncthreads();
+  for (int s = nt / 2; s > 0; s >>= 1) {
+    if (tid < s)
+      for (int q = 0; q < nv; q++) red[q * nt + tid] += red[q * nt + tid + s];
+    __syncthreads();
+  }
+  for (int q = 0; q < nv; q++) v[q] = red[q * nt];
+  __syncthreads();
+}
+
+// Energy terms of one replica at positions X[buf] with the current pair list.
+__device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* red) {
+  const int n = R->n, off = R->off;
+  const long long cap = A.cap;
+  const double* X = A.X[buf];
+  const float4* S = A.stage[buf];
+  double eb = 0, ea = 0, eatt = 0, erep = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const long long gi = off + i;
+    const int4 tp = A.topo[gi];
+    const int nat_cnt = tp.w & 0xFFFF, bnd_cnt = (tp.w >> 16) & 0xFF, ang_cnt = (tp.w >> 24) & 0xFF;
+    const int ti = (int)S[2 * gi].w;
+    if (R->terms & SOP_TERM_FENE)
+      for (int k = 0; k < bnd_cnt; k++) {
+        const int j = A.bnd[tp.y + k].x;
+        if (j <= i) continue;
+        const double d = sqrt(exact_d2(X, cap, gi, off + j));
+        const double dev = d - A.bnd_r0[tp.y + k];
+        eb += log1p(-dev * dev / R->R0sq_d);
+      }
+    if (R->terms & SOP_TERM_ANGLE)
+      for (int k = 0; k < ang_cnt; k++) {
+        const int j = A.ang[tp.z + k];
+        if (j <= i) continue;
+        const double d2 = exact_d2(X, cap, gi, off + j);
+        ea += R->e_ang_coeff / (d2 * d2 * d2);
+      }
+    if (R->terms & SOP_TERM_VDW) {
+      for (int k = 0; k < nat_cnt; k++) {
+        const int4 e = A.nat[tp.x + k];
+        const int j = e.x & (int)kIdx;
+        if (j <= i || !(e.x & (int)kPL)) continue;
+        const int tj = (int)S[2 * (off + (long long)j)].w;
+        const double r0 = A.nat_r0[tp.x + k];
+        const double r2 = r0 * r0, r6 = r2 * r2 * r2, r12 = r6 * r6;
+        const double d2 = exact_d2(X, cap, gi, off + j);
+        const double d6 = d2 * d2 * d2, d12 = d6 * d6;
+        eatt += c_ff.coeff_att[ti][tj] * (r12 / d12) - 2.0 * (r6 / d6);  // energy.cpp:224
+      }
+      const int cnt = A.nl_cnt[gi];
+      const long long row = R->nl_base + (long long)i * R->L;
+      for (int k = 0; k < cnt; k++) {
+        const int e = A.nl[row + k];
+        const int j = e & (int)kIdx;
+        if (j <= i || !(e & (int)kPL)) continue;
+        const int tj = (int)S[2 * (off + (long long)j)].w;
+        const double d2 = exact_d2(X, cap, gi, off + j);
+        const double d6 = d2 * d2 * d2, d12 = d6 * d6;
+        erep += c_ff.coeff_rep[ti][tj] * (c_ff.sigma_rep12[ti][tj] / d12 + c_ff.sigma_rep6[ti][tj] / d6);
+      }
+    }
+  }
+  double v[4] = {eb, ea, eatt, erep};
+  block_sum(v, 4, red);
+  if (threadIdx.x == 0) {
+    R->energy[0] = -R->e_bnd_coeff * v[0];
+    R->energy[1] = v[1];
+    R->energy[3] = v[2];
+    R->energy[4] = v[3];
+    R->energy[2] = v[2] + v[3];
+    R->energy[5] = R->energy[0] + R->energy[1] + R->energy[2];
+  }
+}
+
+// K6: observables (sop.cpp:200-279) at positions X[buf] and the stored velocities.
+__device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red) {
+  const int n = R->n, off = R->off;
+  const long long cap = A.cap;
+  const double* X = A.X[buf];
+  double s[4] = {0, 0, 0, 0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const long long gi = off + i;
+    s[0] += X[gi]; s[1] += X[cap + gi]; s[2] += X[2 * cap + gi];
+  }
+  block_sum(s, 3, red);
+  const double mx = s[0] / n, my = s[1] / n, mz = s[2] / n;
+  double q[4] = {0, 0, 0, 0};  // contacts, natives, sum |r - mean|^2, sum v^2
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const long long gi = off + i;
+    const double ax = X[gi] - mx, ay = X[cap + gi] - my, az = X[2 * cap + gi] - mz;
+    q[2] += ax * ax + ay * ay + az * az;
+    const double vx = A.vel[gi], vy = A.vel[cap + gi], vz = A.vel[2 * cap + gi];
+    q[3] += vx * vx + vy * vy + vz * vz;
+    const int4 tp = A.topo[gi];
+    const int nat_cnt = tp.w & 0xFFFF;
+    for (int k = 0; k < nat_cnt; k++) {
+      const int j = A.nat[tp.x + k].x & (int)kIdx;
+      if (j <= i) continue;
+      const float r_ij = (float)A.nat_r0[tp.x + k];  // sop.cpp:213 reads r0 into a float
+      const double d = sqrt(exact_d2(X, cap, off + j, gi));
+      q[1] += 1.0;
+      if (d / (double)r_ij < 1.25) q[0] += 1.0;
+    }
+  }
+  block_sum(q, 4, red);
+  if (threadIdx.x == 0) {
+    R->obs[1] = q[0];
+    R->obs[0] = q[1] > 0 ? q[0] / q[1] : 0.0;
+    R->obs[2] = q[2] / n;  // sum_{i<j} d^2 / N^2 = sum |r - mean|^2 / N
+    R->obs[3] = q[3] / (3.0 * n);
+    R->obs[4] = sqrt(exact_d2(X, cap, (long long)off, (long long)off + n - 1));
+  }
+}
+
+__global__ void __launch_bounds__(256) k_energy(DevArrays A, const int* rep_ids, int nrep) {
+  __shared__ double red[4 * 256];
+  RepDev* R = &A.rep[rep_ids[blockIdx.x]];
+  replica_energy(A, R, R->cur, red);
+}
+
+__global__ void __launch_bounds__(256) k_obs(DevArrays A, const int* rep_ids, int nrep) {
+  __shared__ double red[4 * 256];
+  RepDev* R = &A.rep[rep_ids[blockIdx.x]];
+  replica_obs(A, R, R->cur, red);
+  if (threadIdx.x == 0) R->obs_pending = 0;
+}
+
+// ---------------------------------------------------------------------------------
+// update_pair_list (sop.cpp:473-553) at the current positions
+
+__global__ void k_pairlist(DevArrays A, int r, int off, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  RepDev* R = &A.rep[r];
+  if (R->mode == SOP_LIST_NONE) return;
+  const long long gi = off + i, cap = A.cap;
+  const double* X = A.X[R->cur];
+  const float4* S = A.stage[R->cur] + 2 * (long long)off;
+  const float4 hi = S[2 * i], lo = S[2 * i + 1];
+  const int ti = (int)hi.w;
+  const int4 tp = A.topo[gi];
+  const int nat_cnt = tp.w & 0xFFFF;
+  for (int k = 0; k < nat_cnt; k++) {
+    const int4 e = A.nat[tp.x + k];
+    const int j = e.x & (int)kIdx;
+    const float4 hj = S[2 * j], lj = S[2 * j + 1];
+    const float dx = (hj.x - hi.x) + (lj.x - lo.x), dy = (hj.y - hi.y) + (lj.y - lo.y),
+                dz = (hj.z - hi.z) + (lj.z - lo.z);
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    bool plb = false;
+    if (e.x & (int)kNL) {
+      const double rc = 2.5 * A.nat_r0[tp.x + k], rc2 = rc * rc;
+      plb = within(d2, (float)rc2, kScreenMargin, [&] { return exact_d2(X, cap, gi, off + j) < rc2; });
+    }
+    A.nat[tp.x + k].x = (e.x & ~(int)kPL) | (plb ? (int)kPL : 0);
+  }
+  const int cnt = A.nl_cnt[gi];
+  const long long row = R->nl_base + (long long)i * R->L;
+  for (int k = 0; k < cnt; k++) {
+    const int e = A.nl[row + k];
+    const int j = e & (int)kIdx;
+    const float4 hj = S[2 * j], lj = S[2 * j + 1];
+    const float dx = (hj.x - hi.x) + (lj.x - lo.x), dy = (hj.y - hi.y) + (lj.y - lo.y),
+                dz = (hj.z - hi.z) + (lj.z - lo.z);
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const int tj = (int)hj.w;
+    const double rc2 = c_ff.rc2_pl[ti][tj];
+    const bool plb =
+        within(d2, (float)rc2, kScreenMargin, [&] { return exact_d2(X, cap, gi, off + j) < rc2; });
+    A.nl[row + k] = (e & ~(int)kPL) | (plb ? (int)kPL : 0);
+  }
+}
+
+// which: 0 neighbor att, 1 neighbor rep, 2 pair att, 3 pair rep
+__global__ void k_export(DevArrays A, int r, int off, int n, int which, int capacity) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const RepDev* R = &A.rep[r];
+  const long long gi = off + i;
+  const int4 tp = A.topo[gi];
+  if (which == 0 || which == 2) {
+    const int nat_cnt = tp.w & 0xFFFF;
+    const unsigned bit = (which == 0) ? kNL : kPL;
+    for (int k = 0; k < nat_cnt; k++) {
+      const int e = A.nat[tp.x + k].x;
+      const int j = e & (int)kIdx;
+      if (j <= i || !((unsigned)e & bit)) continue;
+      const int slot = atomicAdd(A.pairs_cnt, 1);
+      if (slot < capacity) A.pairs_out[slot] = ((unsigned long long)(i + 1) << 32) | (unsigned)(j + 1);
+    }
+  } else {
+    const int cnt = A.nl_cnt[gi];
+    const long long row = R->nl_base + (long long)i * R->L;
+    for (int k = 0; k < cnt; k++) {
+      const int e = A.nl[row + k];
+      const int j = e & (int)kIdx;
+      if (j <= i) continue;
+      if (which == 3 && !((unsigned)e & kPL)) continue;
+      const int slot = atomicAdd(A.pairs_cnt, 1);
+      if (slot < capacity) A.pairs_out[slot] = ((unsigned long long)(i + 1) << 32) | (unsigned)(j + 1);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// launchers
+
+static size_t build_dyn_smem(int max_n) {
+  size_t b = (size_t)max_n * (16 + 4 + 2) + 16, red = 4 * kBuildThreads * sizeof(double);
+  return b > red ? b : red;
+}
+
+// Opt every kernel into the device's full per-block shared memory once.
+template <class K>
+static cudaError_t optin(K kernel, int optin_bytes) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  int dyn = optin_bytes - (int)fa.sharedSizeBytes - 1024;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+}
+
+cudaError_t init_kernels(int optin_bytes) {
+  cudaError_t e;
+  if ((e = optin(k_prologue, optin_bytes)) != cudaSuccess) return e;
+  if ((e = optin(k_step<1>, optin_bytes)) != cudaSuccess) return e;
+  if ((e = optin(k_step<2>, optin_bytes)) != cudaSuccess) return e;
+  if ((e = optin(k_step<4>, optin_bytes)) != cudaSuccess) return e;
+  if ((e = optin(k_step<8>, optin_bytes)) != cudaSuccess) return e;
+  if ((e = optin(k_step<16>, optin_bytes)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, int max_n,
+                            int force_build, int build_mode, int grid, cudaStream_t s) {
+  if (nrep <= 0) return cudaSuccess;
+  size_t dyn = build_dyn_smem(max_n);
+  if (grid <= 0 || grid > nrep) grid = nrep;
+  k_prologue<<<grid, kBuildThreads, dyn, s>>>(A, rep_ids, nrep, force_build, build_mode);
+  return cudaGetLastError();
+}
+
+template <int G>
+static cudaError_t launch_step_g(const DevArrays& A, const StepItem* items, int nitems,
+                                 size_t dyn, int threads, int grid, cudaStream_t s) {
+  k_step<G><<<grid, threads, dyn, s>>>(A, items, nitems);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, int max_staged,
+                        int lanes, int threads, int grid, cudaStream_t s) {
+  if (nitems <= 0) return cudaSuccess;
+  size_t dyn = (size_t)max_staged * 32 + 128;
+  if (grid <= 0) grid = nitems;
+  switch (lanes) {
+    case 1: return launch_step_g<1>(A, items, nitems, dyn, threads, grid, s);
+    case 2: return launch_step_g<2>(A, items, nitems, dyn, threads, grid, s);
+    case 8: return launch_step_g<8>(A, items, nitems, dyn, threads, grid, s);
+    case 16: return launch_step_g<16>(A, items, nitems, dyn, threads, grid, s);
+    default: return launch_step_g<4>(A, items, nitems, dyn, threads, grid, s);
+  }
+}
+
+int step_kernel_max_smem() { return kStageMax * 32 + 128; }
+
+int step_blocks_per_sm(int lanes, int threads, int max_staged) {
+  const size_t dyn = (size_t)max_staged * 32 + 128;
+  int n = 0;
+  cudaError_t e;
+  switch (lanes) {
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<1>, threads, dyn); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<2>, threads, dyn); break;
+    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<8>, threads, dyn); break;
+    case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<16>, threads, dyn); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<4>, threads, dyn); break;
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s) {
+  if (nrep <= 0) return cudaSuccess;
+  k_energy<<<nrep, 256, 0, s>>>(A, rep_ids, nrep);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_observables(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s) {
+  if (nrep <= 0) return cudaSuccess;
+  k_obs<<<nrep, 256, 0, s>>>(A, rep_ids, nrep);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairlist(const DevArrays& A, int r, int off, int n, cudaStream_t s) {
+  k_pairlist<<<(n + 127) / 128, 128, 0, s>>>(A, r, off, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_export(const DevArrays& A, int r, int off, int n, int which, int capacity,
+                          cudaStream_t s) {
+  k_export<<<(n + 127) / 128, 128, 0, s>>>(A, r, off, n, which, capacity);
+  return cudaGetLastError();
+}
+
+}  // namespace sop

@@ -1,0 +1,177 @@
+"""The CPU oracle pinned against the reference (CPU only).
+
+* oracle/sop_oracle.c (the restatement) against oracle/_ref (the unmodified
+  reference sources) on fresh seeded inputs: lists, forces, energies,
+  trajectories and observables bit for bit;
+* the restatement against the committed golden vectors (made by the
+  reference, tests/golden/make_golden.py), which also exist on hosts without
+  the reference tree;
+* the Philox-4x32-10 stream against published known-answer vectors.
+"""
+import glob
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from sop_gb300 import systems as S
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "sop_golden_N*.npz")))
+needs_ref = pytest.mark.skipif(not O.ref_available(), reason="reference tree not built here")
+
+
+def golden_script(mode="neighborlist", temp="0.6", nstep=100, nup=50):
+    return [("set", "zeta", "50"), ("set", "t_step", "0.05"), ("set", "temp", temp),
+            ("set", "nstep", str(nstep)), ("set", "nup", str(nup)),
+            ("set", "cutofftype", mode), ("set", "nnlup", "10"), ("set", "boxl", "500"),
+            ("set", "ncell", "62.5"), ("set", "run", "1")]
+
+
+def system_from_golden(g):
+    return S.System(xyz=g["xyz"], bonds=(g["ib"], g["jb"], g["r0"]),
+                    angles=(g["ia"], g["ja"], g["ka"], g["a0"]),
+                    natives=(g["in_"], g["jn"], g["rn"]), bead_type=np.ones(len(g["xyz"]), np.int32))
+
+
+def port_for(system, script):
+    p = O.Port()
+    p.set_system(system)
+    for _, k, v in script:
+        p.command(k, v)
+    return p
+
+
+def pairs(o, k):
+    ii, jj = o.pairs(k)
+    return np.stack([ii, jj], 1)
+
+
+@needs_ref
+@pytest.mark.parametrize("n,mode", [(30, "neighborlist"), (76, "neighborlist"), (76, "celllist"),
+                                    (120, "none"), (250, "neighborlist")])
+def test_port_equals_reference(n, mode):
+    system = S.synth_chain(5000 + n, n)
+    ref, port = O.Ref(), O.Port()
+    with tempfile.TemporaryDirectory() as d:
+        path = S.write_reference_files(system, d, golden_script(mode), run=False)
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            ref.load_script(path)
+            port.load_script(path)  # file names resolve against the cwd, as in io.cpp
+        finally:
+            os.chdir(cwd)
+    for o in (ref, port):
+        o.set_force_terms(0, 1, 1, 1)
+        o.setup(True)
+    for k in range(4):
+        np.testing.assert_array_equal(pairs(ref, k), pairs(port, k))
+    np.testing.assert_array_equal(ref.energies(), port.energies())
+    np.testing.assert_array_equal(ref.coords(3), port.coords(3))
+    for terms in ((0, 1, 0, 0), (0, 0, 1, 0), (0, 0, 0, 1)):
+        for o in (ref, port):
+            o.set_force_terms(*terms)
+            o.force_eval()
+        np.testing.assert_array_equal(ref.coords(3), port.coords(3))
+    for o in (ref, port):
+        o.set_force_terms(0, 1, 1, 1)
+        o.force_eval()
+        o.run(60)
+        o.energy_eval()
+        o.observables()
+    for which in (1, 2):
+        np.testing.assert_array_equal(ref.coords(which), port.coords(which))
+    np.testing.assert_array_equal(ref.energies(), port.energies())
+    for k in ("Q", "rgsq", "kinT"):
+        assert ref.energy(k) == port.energy(k)
+    for k in range(4):
+        np.testing.assert_array_equal(pairs(ref, k), pairs(port, k))
+
+
+@needs_ref
+def test_reference_files_round_trip():
+    """The vdw file the generator writes splits into exactly the natives it holds."""
+    system = S.synth_chain(77, 60)
+    ref = O.Ref()
+    with tempfile.TemporaryDirectory() as d:
+        path = S.write_reference_files(system, d, golden_script(), run=False)
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            ref.load_script(path)
+        finally:
+            os.chdir(cwd)
+    assert ref.count("ncon_att") == len(system.natives[0])
+    assert ref.count("ncon_att") + ref.count("ncon_rep") == system.candidate_count()
+    np.testing.assert_array_equal(ref.coords(1), system.xyz)
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_port_matches_golden(path):
+    g = np.load(path)
+    system = system_from_golden(g)
+    port = port_for(system, golden_script())
+    np.testing.assert_array_equal([port.param(k) for k in ("T", "zeta", "h", "a1", "a2", "a3", "a4")],
+                                  g["params"])
+    port.set_force_terms(0, 1, 1, 1)
+    port.setup(True)
+    for k, name in enumerate(("nl_att", "nl_rep", "pl_att", "pl_rep")):
+        np.testing.assert_array_equal(pairs(port, k), g[name])
+    # FP64 results: bit-exact on the x86 host that made them; 1e-12 elsewhere
+    np.testing.assert_allclose(port.energies(), g["e0"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(port.coords(3), g["f_all"], rtol=1e-11, atol=1e-11)
+    for name, terms in (("f_fene", (0, 1, 0, 0)), ("f_ang", (0, 0, 1, 0)), ("f_vdw", (0, 0, 0, 1))):
+        port.set_force_terms(*terms)
+        port.force_eval()
+        np.testing.assert_allclose(port.coords(3), g[name], rtol=1e-11, atol=1e-11)
+    port.set_force_terms(0, 1, 1, 1)
+    port.force_eval()
+    port.run(100)
+    port.energy_eval()
+    port.observables()
+    np.testing.assert_allclose(port.coords(1), g["traj_unc"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(port.coords(2), g["traj_vel"], rtol=0, atol=1e-8)
+    np.testing.assert_allclose(port.energies(), g["traj_e"], rtol=1e-10, atol=1e-10)
+    obs = [port.energy("Q"), port.count("contct_nat"), port.energy("rgsq"), port.energy("kinT")]
+    np.testing.assert_allclose(obs, g["traj_obs"], rtol=1e-10)
+    for k, name in enumerate(("nl_att", "nl_rep", "pl_att", "pl_rep")):
+        np.testing.assert_array_equal(pairs(port, k), g["traj_" + name])
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_port_cell_list_matches_golden(path):
+    g = np.load(path)
+    port = port_for(system_from_golden(g), golden_script("celllist"))
+    port.setup(False)
+    for k, name in enumerate(("nl_att", "nl_rep", "pl_att", "pl_rep")):
+        np.testing.assert_array_equal(pairs(port, k), g["cell_" + name])
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_port_steepest_descent_matches_reference_program(path):
+    """sop.x at T=0 (v stays 0, x += a2 F, sop.cpp:316) against update.out."""
+    g = np.load(path)
+    port = port_for(system_from_golden(g), golden_script(temp="0.0"))
+    port.setup(True)
+    for row in g["sd_update"]:
+        step = int(row[0])
+        port.run(step - int(port.param("force_evals")) + 1)
+        port.energy_eval()
+        port.observables()
+        got = [port.energy("kinT"), port.energy("e_bnd"), port.energy("e_ang_ss"),
+               port.energy("e_vdw_rr"), port.energy("rna_etot"), port.energy("Q"),
+               port.count("contct_nat"), port.energy("rgsq")]
+        np.testing.assert_allclose(got, row[2:], rtol=0, atol=2e-6)  # %f columns
+    np.testing.assert_allclose(port.coords(1), g["sd_unc"], rtol=0, atol=2e-6)
+
+
+def test_philox_known_answers():
+    """Random123 known-answer vectors for Philox-4x32-10."""
+    kat = [((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+           ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+           ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+            (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
+    for ctr, key, want in kat:
+        assert tuple(O.philox(ctr, key)) == want
