@@ -117,6 +117,10 @@ typedef struct sop_engine_config {
   int block_threads;     /* fused step kernel block size (0 = 256)            */
   int lanes_per_bead;    /* lanes cooperating on one bead: 1,2,4,8 (0 = 4)     */
   int graph_steps;       /* steps captured per CUDA graph launch (0 = 20)      */
+  int stage_limit;       /* largest replica (beads) whose positions the step
+                            kernel stages in shared memory by TMA; larger ones
+                            are gathered through L1 (0 = 6144, <0 = never)    */
+  int chunk_beads;       /* beads per step-kernel work item (0 = 256)          */
 } sop_engine_config;
 
 /* ---- engine -------------------------------------------------------------- */
@@ -145,6 +149,9 @@ int sop_replica_get_state(sop_engine* e, int replica, double* pos, double* unc_p
 /* overwrite unc_pos (and pos) and velocities; vel NULL = zero */
 int sop_replica_set_state(sop_engine* e, int replica, const double* unc_pos, const double* vel);
 int sop_replica_status(sop_engine* e, int replica, int* status, int64_t* steps_done);
+/* diagnostics: out[0..7] = nbead, list row capacity L, longest row at the last
+ * build, list builds so far, iteration t, status bits, native pairs, offset */
+int sop_replica_info(sop_engine* e, int replica, int64_t* out);
 int sop_replica_count(const sop_engine* e, int* n);
 
 /* ---- reference-named operations on one replica (synchronous) -------------- */

@@ -49,6 +49,7 @@ static FFTables make_tables() {
       t.s2[i][j] = (float)t.sigma_rep2[i][j];
       double rpl = 2.5 * sr[i][j];  // sop.cpp:539-540
       t.rc2_pl[i][j] = rpl * rpl;
+      t.rc2_pl_f[i][j] = (float)t.rc2_pl[i][j];
       double rnl = 3.2 * sr[i][j];  // neighbor_list.cpp:97-100
       t.rc2_nl[i][j] = rnl * rnl;
     }
@@ -187,6 +188,8 @@ extern "C" void sop_engine_config_default(sop_engine_config* c) {
   c->block_threads = 256;
   c->lanes_per_bead = 4;
   c->graph_steps = 20;
+  c->stage_limit = kStageMax;
+  c->chunk_beads = 256;
 }
 
 // ---- engine lifetime ------------------------------------------------------------
@@ -209,7 +212,11 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
     if (cfg_in->block_threads > 0) cfg.block_threads = cfg_in->block_threads;
     if (cfg_in->lanes_per_bead > 0) cfg.lanes_per_bead = cfg_in->lanes_per_bead;
     if (cfg_in->graph_steps > 0) cfg.graph_steps = cfg_in->graph_steps;
+    if (cfg_in->stage_limit != 0) cfg.stage_limit = cfg_in->stage_limit;
+    if (cfg_in->chunk_beads > 0) cfg.chunk_beads = cfg_in->chunk_beads;
   }
+  if (cfg.stage_limit > kStageMax) cfg.stage_limit = kStageMax;
+  if (cfg.chunk_beads < 32) cfg.chunk_beads = 32;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
     cudaGetLastError();
@@ -256,6 +263,14 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(dalloc(&A.pairs_cnt, 1));
   CK(dalloc(&A.err, 1));
   CK(cudaMemsetAsync(A.err, 0, sizeof(int), e->stream));
+  // unit queue: every replica may queue all its build slices plus two units
+  A.unit_cap = cfg.max_replicas * (kBuildMax / kSliceBeads + 2);
+  CK(dalloc(&A.units, A.unit_cap));
+  CK(dalloc(&A.unit_cnt, 2));
+  A.unit_exit = A.unit_cnt + 1;
+  CK(dalloc(&A.slice_done, cfg.max_replicas));
+  CK(cudaMemsetAsync(A.unit_cnt, 0, 2 * sizeof(int), e->stream));
+  CK(cudaMemsetAsync(A.slice_done, 0, sizeof(int) * cfg.max_replicas, e->stream));
   CK(cudaMemsetAsync(A.rep, 0, sizeof(RepDev) * cfg.max_replicas, e->stream));
   CK(dalloc(&e->d_ids, cfg.max_replicas + 4));
   CK(dalloc(&e->d_items, cap / 32 + cfg.max_replicas + 16));
@@ -285,7 +300,8 @@ extern "C" int sop_engine_destroy(sop_engine* e) {
   DevArrays& A = e->A;
   void* ptrs[] = {A.X[0], A.X[1], A.stage[0], A.stage[1], A.incr, A.vel, A.force, A.xb, A.topo,
                   A.exc_rng, A.nl_cnt, A.nl, A.nat, A.nat_r0, A.bnd, A.bnd_r0, A.ang, A.exc,
-                  A.rep, A.pairs_out, A.pairs_cnt, A.err, e->d_ids, e->d_items};
+                  A.rep, A.pairs_out, A.pairs_cnt, A.err, A.units, A.unit_cnt, A.slice_done,
+                  e->d_ids, e->d_items};
   for (void* p : ptrs) cudaFree(p);
   if (e->h_rep) cudaFreeHost(e->h_rep);
   for (int k = 0; k < 4; k++) if (e->ev[k]) cudaEventDestroy(e->ev[k]);
@@ -605,7 +621,9 @@ int sop::build_now(sop_engine* e, int r, int mode) {
   int id = r;
   CK(cudaMemcpyAsync(e->d_ids + scratch_id(e, 0), &id, sizeof(int), cudaMemcpyHostToDevice,
                      e->stream));
-  CK(launch_prologue(e->A, e->d_ids + scratch_id(e, 0), 1, R.n, 1, mode, 1, e->stream));
+  const int nsl = (R.n + kSliceBeads - 1) / kSliceBeads;
+  CK(launch_prologue(e->A, e->d_ids + scratch_id(e, 0), 1, R.n, 1, mode,
+                     std::min(nsl, 2 * e->prop.multiProcessorCount), e->stream));
   e->launches++;
   CK(cudaStreamSynchronize(e->stream));
   return SOP_OK;
@@ -676,6 +694,8 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
   CK(cudaMemsetAsync(e->A.nl_cnt + off, 0, sizeof(int) * n, e->stream));
   rd.off = (int)off;
   rd.n = n;
+  rd.type_mask = 0;
+  for (int t : T.type) rd.type_mask |= 1 << t;
   rd.nl_base = nlb;
   rd.L = L;
   rd.nat_base = (int)nb; rd.bnd_base = (int)bb; rd.ang_base = (int)ab; rd.exc_base = (int)xb;
@@ -832,7 +852,35 @@ extern "C" int sop_replica_status(sop_engine* e, int r, int* status, int64_t* st
   return SOP_OK;
 }
 
+extern "C" int sop_replica_info(sop_engine* e, int r, int64_t* out) {
+  if (!e || !out || !live(e, r)) return SOP_ERR_ARG;
+  RepDev d;
+  int rc = get_rep(e, r, &d);
+  if (rc) return rc;
+  const Replica& R = e->reps[r];
+  out[0] = R.n;
+  out[1] = R.L;
+  out[2] = d.max_row;
+  out[3] = d.builds;
+  out[4] = d.t;
+  out[5] = d.status;
+  out[6] = R.nnat_pairs;
+  out[7] = R.off;
+  return SOP_OK;
+}
+
 // ---- layout of the batched step -------------------------------------------------
+
+// Step-kernel work items of one replica: chunks of cfg.chunk_beads beads,
+// staged through shared memory when the replica fits the stage limit.
+static std::vector<StepItem> replica_items(const sop_engine* e, int r) {
+  const Replica& R = e->reps[r];
+  const int chunk = e->cfg.chunk_beads;
+  const int staged = e->cfg.stage_limit > 0 && R.n <= e->cfg.stage_limit;
+  std::vector<StepItem> items;
+  for (int b = 0; b < R.n; b += chunk) items.push_back(StepItem{r, b, std::min(R.n, b + chunk), staged});
+  return items;
+}
 
 int sop::refresh_layout(sop_engine* e) {
   if (!e->layout_dirty) return SOP_OK;
@@ -844,13 +892,12 @@ int sop::refresh_layout(sop_engine* e) {
   e->max_n = 0;
   e->max_staged = 0;
   e->items.clear();
-  const int chunk = e->chunk_beads;
   for (int r : ids) {
     const Replica& R = e->reps[r];
     e->max_n = std::max(e->max_n, R.n);
-    const int staged = R.n <= kStageMax;
-    if (staged) e->max_staged = std::max(e->max_staged, R.n);
-    for (int b = 0; b < R.n; b += chunk) e->items.push_back(StepItem{r, b, std::min(R.n, b + chunk), staged});
+    std::vector<StepItem> it = replica_items(e, r);
+    if (it[0].staged) e->max_staged = std::max(e->max_staged, R.n);
+    e->items.insert(e->items.end(), it.begin(), it.end());
   }
   if ((long long)e->items.size() > e->items_cap) return SOP_ERR_FULL;
   if (!ids.empty()) CK(h2d(e->d_ids, ids.data(), ids.size(), e->stream));
@@ -859,7 +906,7 @@ int sop::refresh_layout(sop_engine* e) {
   // persistent grid: as many CTAs as fit at once, at most one per item
   const int per_sm = step_blocks_per_sm(e->cfg.lanes_per_bead, e->cfg.block_threads, e->max_staged);
   e->step_grid = std::max(1, std::min((int)e->items.size(), per_sm * e->prop.multiProcessorCount));
-  e->pro_grid = std::max(1, std::min((int)ids.size(), e->prop.multiProcessorCount * 2));
+  e->pro_grid = e->prop.multiProcessorCount * 2;  // k_build CTAs over the unit queue
   e->layout_dirty = false;
   e->graph_valid = false;
   return SOP_OK;
@@ -908,9 +955,8 @@ extern "C" int sop_run_plain(sop_engine* e, int r, int64_t nsteps) {
   CK(cudaSetDevice(e->cfg.device));
   // per-replica id and items (kept at the top of the id / item arrays)
   const int id_slot = scratch_id(e, 1);
-  std::vector<StepItem> items;
-  const int staged = R.n <= kStageMax;
-  for (int b = 0; b < R.n; b += e->chunk_beads) items.push_back(StepItem{r, b, std::min(R.n, b + e->chunk_beads), staged});
+  const std::vector<StepItem> items = replica_items(e, r);
+  const int staged = items[0].staged;
   const long long item_slot = e->items_cap - (long long)items.size();
   if (item_slot < (long long)e->items.size()) return SOP_ERR_FULL;
   CK(cudaMemcpyAsync(e->d_ids + id_slot, &r, sizeof(int), cudaMemcpyHostToDevice, e->stream));
@@ -920,9 +966,10 @@ extern "C" int sop_run_plain(sop_engine* e, int r, int64_t nsteps) {
   CK(cudaGetLastError());
   CK(cudaEventRecord(e->ev[0], e->stream));
   const int grid = std::min((int)items.size(), 4 * e->prop.multiProcessorCount);
+  const int bgrid = std::min((R.n + kSliceBeads - 1) / kSliceBeads + 1, 2 * e->prop.multiProcessorCount);
   for (int64_t s = 0; s <= nsteps; s++) {
     int rc = enqueue_step(e, e->d_ids + id_slot, 1, e->d_items + item_slot, (int)items.size(), R.n,
-                          staged ? R.n : 0, grid, 1);
+                          staged ? R.n : 0, grid, bgrid);
     if (rc) return rc;
   }
   CK(launch_observables(e->A, e->d_ids + id_slot, 1, e->stream));
@@ -1121,9 +1168,8 @@ extern "C" int sop_get_pair_list(sop_engine* e, int r, int which, int* ii, int* 
 
 static int run_phase(sop_engine* e, int r, int phase) {
   Replica& R = e->reps[r];
-  std::vector<StepItem> items;
-  const int staged = R.n <= kStageMax;
-  for (int b = 0; b < R.n; b += e->chunk_beads) items.push_back(StepItem{r, b, std::min(R.n, b + e->chunk_beads), staged});
+  const std::vector<StepItem> items = replica_items(e, r);
+  const int staged = items[0].staged;
   const long long item_slot = e->items_cap - (long long)items.size();
   CK(h2d(e->d_items + item_slot, items.data(), items.size(), e->stream));
   k_set_phase<<<1, 1, 0, e->stream>>>(e->A.rep, r, phase);

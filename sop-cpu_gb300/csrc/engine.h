@@ -66,7 +66,6 @@ struct sop_engine {
   std::vector<int> active;
   std::vector<sop::StepItem> items;
   int max_n = 0, max_staged = 0, step_grid = 1, pro_grid = 1;
-  int chunk_beads = 256;
   bool layout_dirty = true;
   // CUDA graph of graph_steps batched steps
   cudaGraphExec_t graph_exec = nullptr;

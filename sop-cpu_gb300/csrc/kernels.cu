@@ -1,10 +1,14 @@
 // GB300 kernels of the SOP hot path.
 //
-//   k_prologue  per-replica step bookkeeping (phase, noise counter, the
-//               reference's nnlup cadence) and, when due, the list build:
-//               K1 cell binning (warp-match counting sort, stable by bead) and
-//               K2 neighbor/pair-list build over the 27-cell stencil, cutoffs
-//               decided bit-exactly against the reference's FP64 arithmetic.
+//   k_decide    per-replica step bookkeeping (phase, noise counter, the
+//               reference's nnlup cadence or the displacement trigger) that
+//               queues the step's due work units.
+//   k_build     persistent CTAs over those units: list builds in 128-bead
+//               slices -- K1 cell binning (warp-match counting sort, stable by
+//               bead) and K2 neighbor/pair-list build over the 27-cell stencil,
+//               one warp per bead, cutoffs decided bit-exactly against the
+//               reference's FP64 arithmetic -- and output-step energies and
+//               observables.
 //   k_step      K3+K4 fused: pair/bond/angle forces in FP32 from positions
 //               staged in shared memory by TMA bulk copies, lane partials to
 //               int64 fixed point and reduced with warp shuffles, counter-
@@ -147,9 +151,14 @@ __device__ __forceinline__ void fence_async_smem() {
 // ---------------------------------------------------------------------------------
 // K1 + K2: list build of one replica by one CTA (n <= kBuildMax)
 
+constexpr int kWarpNat = 64;  // native partners per bead staged per warp
+
 struct BuildSmem {
   int cstart[kMaxCells + 1];
   int ccur[kMaxCells];
+  int wnat[kBuildThreads / 32][kWarpNat];
+  int wbeg[kBuildThreads / 32][32];
+  int wpre[kBuildThreads / 32][32];
   float red[6][32];
   int s_ok, s_nx, s_ny, s_nz, s_maxrow, s_status;
   float s_edge, s_ox, s_oy, s_oz;
@@ -168,10 +177,12 @@ __device__ __forceinline__ int bsearch_sorted(const int* a, int n, int key) {
   return -1;
 }
 
-// Build the replica's lists from position buffer `src` in list mode `mode`.
+// Build the lists of beads [b0, b1) of replica r from position buffer `src`
+// in list mode `mode`.  Every slice bins the whole replica (O(n)) and then
+// enumerates its own beads, so slices of one replica run on different CTAs.
 // Dynamic shared memory: float4 P[n] | int sorted[n] | ushort cell[n].
-__device__ void build_lists(const DevArrays& A, int r, int src, int mode, BuildSmem& B,
-                            unsigned char* dyn) {
+__device__ void build_lists(const DevArrays& A, int r, int src, int mode, int b0, int b1,
+                            BuildSmem& B, unsigned char* dyn) {
   RepDev* R = &A.rep[r];
   const int n = R->n, off = R->off, tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
@@ -184,10 +195,13 @@ __device__ void build_lists(const DevArrays& A, int r, int src, int mode, BuildS
   const double boxl = R->boxl;
   const float skin = R->skin;
 
-  // list cutoff per type pair (non-natives) and the largest one
+  // list cutoff per type pair (non-natives) and the largest one over the
+  // bead types present in this replica
   float rl_max = 0.f;
+  const int tmask = R->type_mask ? R->type_mask : 0x6;
   for (int a = 1; a < kMaxTypes; a++)
     for (int b = 1; b < kMaxTypes; b++) {
+      if (!((tmask >> a) & 1) || !((tmask >> b) & 1)) continue;
       float rl = (mode == SOP_LIST_SKIN) ? (float)(2.5 * c_ff.sigma_rep[a][b]) + skin
                                          : (float)(3.2 * c_ff.sigma_rep[a][b]);
       rl_max = fmaxf(rl_max, rl);
@@ -345,12 +359,18 @@ __device__ void build_lists(const DevArrays& A, int r, int src, int mode, BuildS
   }
   __syncthreads();
 
-  // 4. neighbor enumeration: one thread per bead, stencil in fixed order
+  // 4. neighbor enumeration: one warp per bead; the lanes test 32 stencil
+  // candidates at a time and ballot-compact the survivors, so each row holds
+  // its partners in stencil order, bead order within a cell (deterministic).
   const long long nl_base = R->nl_base;
   const int L = R->L;
   const float margin = 1e-5f;
   int my_status = 0, my_max = 0;
-  for (int i = tid; i < n; i += nt) {
+  int* wnat = B.wnat[warp];
+  int* wbeg = B.wbeg[warp];  // first sorted slot of each stencil cell
+  int* wpre = B.wpre[warp];  // exclusive prefix of the stencil-cell counts
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int i = b0 + warp; i < b1; i += nwarp) {
     const float4 pi = P[i];
     const int code_i = (int)pi.w, ti = code_i & 3, chi = code_i >> 2;
     const int c = cell[i];
@@ -360,77 +380,113 @@ __device__ void build_lists(const DevArrays& A, int r, int src, int mode, BuildS
     const int2 er = A.exc_rng[off + i];
     const long long row = nl_base + (long long)i * L;
     const long long gi = off + i;
-    // list cutoff^2 against partner type 1 and 2 (neighbor_list.cpp:97-100, or 2.5 sigma + skin)
-    double rl2d[kMaxTypes];
-    float rl2f[kMaxTypes];
+    // the bead's native partners (sorted) staged for the exclusion test
+    const bool nat_in_smem = nat_cnt <= kWarpNat;
+    if (nat_in_smem)
+      for (int k = lane; k < nat_cnt; k += 32) wnat[k] = A.nat[tp.x + k].x & (int)kIdx;
+    __syncwarp();
+    double rl2d[kMaxTypes], pl2d[kMaxTypes];
+    float rl2f[kMaxTypes], pl2f[kMaxTypes];
     for (int t = 1; t < kMaxTypes; t++) {
       double rl = 2.5 * c_ff.sigma_rep[ti][t] + (double)skin;
       rl2d[t] = (mode == SOP_LIST_SKIN) ? rl * rl : c_ff.rc2_nl[ti][t];
       rl2f[t] = (float)rl2d[t];
+      pl2d[t] = c_ff.rc2_pl[ti][t];  // (2.5 sigma)^2, sop.cpp:539-541
+      pl2f[t] = (float)pl2d[t];
     }
     rl2d[0] = rl2d[1];
     rl2f[0] = rl2f[1];
-    int cnt = 0;
-    for (int dz = -1; dz <= 1; dz++) {
-      int zz = cz + dz;
-      if (zz < 0 || zz >= nz) continue;
-      for (int dy = -1; dy <= 1; dy++) {
-        int yy = cy + dy;
-        if (yy < 0 || yy >= ny) continue;
-        for (int dx = -1; dx <= 1; dx++) {
-          int xx = cx + dx;
-          if (xx < 0 || xx >= nx) continue;
-          int cc = xx + nx * (yy + ny * zz);
-          for (int s = B.cstart[cc], e = B.cstart[cc + 1]; s < e; s++) {
-            int j = sorted[s];
-            if (j == i) continue;
-            float4 pj = P[j];
-            int code_j = (int)pj.w, tj = code_j & 3, chj = code_j >> 2;
-            if (chi == chj && abs(i - j) <= 2) continue;
-            float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
-            float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
-            const long long gj = off + j;
-            bool inl, inp;
-            if (mode == SOP_LIST_NONE || mode == SOP_LIST_CELL) {
-              inl = true;  // cell adjacency is the whole predicate (cell_list.cpp:86-88)
-            } else {
-              // cheap rejection first: most stencil candidates lie outside the list sphere
-              if (d2 > rl2f[tj] * (1.0f + margin)) continue;
-              const double rl2 = rl2d[tj];
-              inl = within(d2, (float)rl2, margin, [&] { return exact_d2(X, cap, gi, gj) < rl2; });
+    pl2d[0] = pl2d[1];
+    pl2f[0] = pl2f[1];
+    // the 27 stencil cells (dz, dy, dx from -1 to 1) flattened into one
+    // candidate range: lane k < 27 owns cell k, a warp scan gives offsets
+    int ccount = 0, cbeg = 0;
+    if (lane < 27) {
+      const int xx = cx + lane % 3 - 1, yy = cy + (lane / 3) % 3 - 1, zz = cz + lane / 9 - 1;
+      if (xx >= 0 && xx < nx && yy >= 0 && yy < ny && zz >= 0 && zz < nz) {
+        const int cc = xx + nx * (yy + ny * zz);
+        cbeg = B.cstart[cc];
+        ccount = B.cstart[cc + 1] - cbeg;
+      }
+    }
+    int incl = ccount;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    wbeg[lane] = cbeg;
+    wpre[lane] = incl - ccount;
+    __syncwarp();
+    int cnt = 0;  // warp-uniform
+    {
+      {
+        {
+          for (int base = 0; base < total; base += 32) {
+            const int f = base + lane;
+            bool pass = f < total;
+            int j = 0, tj = 1;
+            float d2 = 0.f;
+            if (pass) {
+              int lo = 0, hi = 26;  // last stencil cell whose prefix <= f
+              while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (wpre[mid] <= f) lo = mid;
+                else hi = mid - 1;
+              }
+              j = sorted[wbeg[lo] + (f - wpre[lo])];
+              const float4 pj = P[j];
+              const int code_j = (int)pj.w, chj = code_j >> 2;
+              tj = code_j & 3;
+              pass = j != i && !(chi == chj && abs(i - j) <= 2);
+              const float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
+              d2 = ddx * ddx + ddy * ddy + ddz * ddz;
             }
-            if (!inl) continue;
-            // natives are listed separately (sorted by partner)
-            bool is_nat = false;
-            {
+            const long long gj = off + j;
+            if (pass && mode != SOP_LIST_NONE && mode != SOP_LIST_CELL) {
+              // cell adjacency is the whole predicate in cell mode (cell_list.cpp:86-88)
+              const double rl2 = rl2d[tj];
+              pass = d2 <= rl2f[tj] * (1.0f + margin) &&
+                     within(d2, rl2f[tj], margin, [&] { return exact_d2(X, cap, gi, gj) < rl2; });
+            }
+            if (pass) {  // natives are listed separately (sorted by partner)
               int lo = 0, hi = nat_cnt;
               while (lo < hi) {
-                int mid = (lo + hi) >> 1;
-                int v = A.nat[tp.x + mid].x & (int)kIdx;
-                if (v == j) { is_nat = true; break; }
+                const int mid = (lo + hi) >> 1;
+                const int v = nat_in_smem ? wnat[mid] : (A.nat[tp.x + mid].x & (int)kIdx);
+                if (v == j) { pass = false; break; }
                 if (v < j) lo = mid + 1;
                 else hi = mid;
               }
             }
-            if (is_nat) continue;
-            if (er.y > 0 && bsearch_sorted(A.exc + er.x, er.y, j) >= 0) continue;
-            if (mode == SOP_LIST_NONE) {
-              inp = true;  // no pair-list filter without a cutoff type
-            } else {
-              double rc2 = c_ff.rc2_pl[ti][tj];
-              inp = within(d2, (float)rc2, margin, [&] { return exact_d2(X, cap, gi, gj) < rc2; });
+            if (pass && er.y > 0 && bsearch_sorted(A.exc + er.x, er.y, j) >= 0) pass = false;
+            bool inp = false;
+            if (pass) {
+              if (mode == SOP_LIST_NONE) {
+                inp = true;  // no pair-list filter without a cutoff type
+              } else {
+                const double rc2 = pl2d[tj];
+                inp = within(d2, pl2f[tj], margin, [&] { return exact_d2(X, cap, gi, gj) < rc2; });
+              }
             }
-            if (cnt < L) A.nl[row + cnt] = j | (inp ? (int)kPL : 0);
-            cnt++;
+            const unsigned m = __ballot_sync(0xffffffffu, pass);
+            const int pos = cnt + __popc(m & lt_mask);
+            if (pass && pos < L) A.nl[row + pos] = j | (inp ? (int)kPL : 0);
+            cnt += __popc(m);
           }
         }
       }
     }
-    if (cnt > L) my_status |= SOP_ST_LIST_OVERFLOW;
-    my_max = max(my_max, cnt);
-    A.nl_cnt[off + i] = min(cnt, L);
-    // natives: neighbor-list and pair-list bits
-    for (int k = 0; k < nat_cnt; k++) {
+    if (lane == 0) {
+      if (cnt > L) my_status |= SOP_ST_LIST_OVERFLOW;
+      my_max = max(my_max, cnt);
+      A.nl_cnt[off + i] = min(cnt, L);
+      const float4 h = S[2 * i];
+      A.xb[off + i] = make_float4(h.x, h.y, h.z, 0.f);
+    }
+    __syncwarp();
+    // natives: neighbor-list and pair-list bits, one lane per native entry
+    for (int k = lane; k < nat_cnt; k += 32) {
       int4 e = A.nat[tp.x + k];
       int j = e.x & (int)kIdx;
       float4 pj = P[j];
@@ -459,16 +515,13 @@ __device__ void build_lists(const DevArrays& A, int r, int src, int mode, BuildS
       }
       A.nat[tp.x + k].x = j | (nlb ? (int)kNL : 0) | (plb ? (int)kPL : 0);
     }
-    float4 h = S[2 * i];
-    A.xb[off + i] = make_float4(h.x, h.y, h.z, 0.f);
+    __syncwarp();
   }
   atomicMax(&B.s_maxrow, my_max);
   if (my_status) atomicOr(&B.s_status, my_status);
   __syncthreads();
   if (tid == 0) {
-    R->max_row = B.s_maxrow;
-    R->builds += 1;
-    R->rebuild = 0;
+    atomicMax(&R->max_row, B.s_maxrow);
     if (B.s_status) atomicOr(&R->status, B.s_status);
   }
 }
@@ -476,84 +529,132 @@ __device__ void build_lists(const DevArrays& A, int r, int src, int mode, BuildS
 __device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* red);
 __device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red);
 
-// Per-replica step bookkeeping.  CTA b handles replica ids b, b+grid, ...:
-// one thread per replica first decides the step (phase, noise counter, the
-// reference's nnlup cadence or the displacement trigger, output), then the
-// CTA does that replica's due work in order:
+// Work units queued by k_decide for k_build: {replica, kind | mode << 8, slice, buffer}.
+enum UnitKind : int { U_OBS = 1, U_BUILD = 2, U_ENERGY = 3 };
+
+__device__ __forceinline__ void push_units(const DevArrays& A, int r, int kind, int mode, int nsl,
+                                           int buf) {
+  const int base = atomicAdd(A.unit_cnt, nsl);
+  for (int s = 0; s < nsl; s++)
+    if (base + s < A.unit_cap) A.units[base + s] = make_int4(r, kind | (mode << 8), s, buf);
+}
+
+// Per-replica step bookkeeping, one thread per replica: phase, noise counter,
+// the reference's nnlup cadence or the displacement trigger, output steps.
+// Due work goes to the unit queue, in this order of meaning:
 //   observables of the previous output step (positions X_{t-1}, velocities v_{t-1}),
-//   the list build from X_{t-1} (sop.cpp:156-170: rebuild before the step),
-//   the energies of this output step at X_t with pair list PL_t.
-// Energies must precede the step kernel, which rewrites the pair-list bits.
-__global__ void __launch_bounds__(kBuildThreads, 1) k_prologue(DevArrays A, const int* rep_ids,
-                                                            int nrep, int force_build,
-                                                            int build_mode) {
+//   the list build from X_{t-1} in slices (sop.cpp:156-170: rebuild before the step),
+//   the energies of this output step at X_t with pair list PL_t (after the build,
+//   before the step kernel rewrites the pair-list bits).
+__global__ void k_decide(DevArrays A, const int* rep_ids, int nrep, int force_build, int build_mode) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nrep) return;
+  const int r = rep_ids[k];
+  RepDev* R = &A.rep[r];
+  RepDev Q = *R;  // one pipelined copy; decide in registers, store back
+  const int nsl = (Q.n + kSliceBeads - 1) / kSliceBeads;
+  if (force_build) {
+    A.slice_done[r] = 0;
+    R->max_row = 0;
+    R->en_after = 0;
+    push_units(A, r, U_BUILD, build_mode, nsl, Q.cur);
+    return;
+  }
+  if (Q.obs_pending) {
+    push_units(A, r, U_OBS, 0, 1, Q.cur);
+    R->obs_pending = 0;
+  }
+  if (!Q.active || !Q.running ||
+      (Q.status & (SOP_ST_NONFINITE | SOP_ST_LIST_OVERFLOW | SOP_ST_PERIODIC | SOP_ST_GRID))) {
+    R->phase = PH_SKIP;
+    R->out = 0;
+    return;
+  }
+  bool need = false;
+  const int prev = Q.cur;
+  if (Q.moved) {
+    if (Q.mode == SOP_LIST_NEIGHBOR || Q.mode == SOP_LIST_CELL) {
+      // underdamped_ctrl cadence (sop.cpp:156-165), local inlup from 1
+      if (Q.inlup % Q.nnlup == 0) { need = true; Q.inlup = 0; }
+      Q.inlup++;
+      R->inlup = Q.inlup;
+    } else if (Q.mode == SOP_LIST_SKIN) {
+      need = Q.rebuild != 0;
+    }
+    Q.cur ^= 1;
+    Q.moved = 0;
+  }
+  int ph;
+  if (Q.first_pending) { ph = PH_FIRST; R->first_pending = 0; }
+  else if (Q.t >= Q.t_end) ph = PH_FINAL;
+  else ph = PH_NORMAL;
+  R->t_cur = Q.t;
+  if (ph == PH_FINAL) {
+    R->running = 0;
+  } else {
+    R->t = Q.t + 1;
+    Q.moved = 1;
+  }
+  R->cur = Q.cur;
+  R->moved = Q.moved;
+  R->phase = ph;
+  const int out = (ph == PH_NORMAL || ph == PH_FINAL) && Q.nup > 0 && Q.t > 0 && (Q.t % Q.nup) == 0;
+  R->out = out;
+  if (out) R->obs_pending = 1;
+  R->en_after = need && out;
+  if (need) {
+    A.slice_done[r] = 0;
+    R->max_row = 0;
+    push_units(A, r, U_BUILD, Q.mode, nsl, prev);
+  }
+  if (out && !need) push_units(A, r, U_ENERGY, 0, 1, Q.cur);
+}
+
+// Persistent CTAs over the unit queue.  The CTA that finishes the last slice
+// of a build closes it (counters, displacement flag) and, on an output step,
+// computes the energies with the new pair list.  The last CTA to exit resets
+// the queue for the next step.
+__global__ void __launch_bounds__(kBuildThreads, 1) k_build(DevArrays A) {
   extern __shared__ __align__(16) unsigned char dyn[];
   __shared__ BuildSmem B;
-  __shared__ int s_obs[64], s_build[64], s_en[64], s_prev[64], s_cur[64], s_mode[64];
+  __shared__ int s_last;
   double* red = reinterpret_cast<double*>(dyn);
-  const int per = (nrep + gridDim.x - 1) / gridDim.x;
-  for (int chunk = 0; chunk < per; chunk += 64) {
-    const int tid = threadIdx.x;
-    if (tid < 64) {
-      s_obs[tid] = s_build[tid] = s_en[tid] = 0;
-      int k = blockIdx.x + (chunk + tid) * gridDim.x;
-      if (chunk + tid < per && k < nrep) {
-        RepDev* R = &A.rep[rep_ids[k]];
-        s_prev[tid] = s_cur[tid] = R->cur;
-        s_mode[tid] = R->mode;
-        if (force_build) {
-          s_build[tid] = 1;
-          s_mode[tid] = build_mode;
-        } else {
-          if (R->obs_pending) { s_obs[tid] = 1; R->obs_pending = 0; }
-          if (!R->active || !R->running ||
-              (R->status & (SOP_ST_NONFINITE | SOP_ST_LIST_OVERFLOW | SOP_ST_PERIODIC | SOP_ST_GRID))) {
-            R->phase = PH_SKIP;
-            R->out = 0;
-          } else {
-            if (R->moved) {
-              bool need = false;
-              if (R->mode == SOP_LIST_NEIGHBOR || R->mode == SOP_LIST_CELL) {
-                // underdamped_ctrl cadence (sop.cpp:156-165), local inlup from 1
-                if (R->inlup % R->nnlup == 0) { need = true; R->inlup = 0; }
-                R->inlup++;
-              } else if (R->mode == SOP_LIST_SKIN) {
-                need = R->rebuild != 0;
-              }
-              s_build[tid] = need;
-              R->cur ^= 1;
-              R->moved = 0;
-            }
-            int ph;
-            if (R->first_pending) { ph = PH_FIRST; R->first_pending = 0; }
-            else if (R->t >= R->t_end) ph = PH_FINAL;
-            else ph = PH_NORMAL;
-            R->t_cur = R->t;
-            if (ph == PH_FINAL) {
-              R->running = 0;
-            } else {
-              R->t += 1;
-              R->moved = 1;
-            }
-            R->phase = ph;
-            R->out = (ph == PH_NORMAL || ph == PH_FINAL) && R->nup > 0 && R->t_cur > 0 &&
-                     (R->t_cur % R->nup) == 0;
-            if (R->out) { s_en[tid] = 1; R->obs_pending = 1; }
-            s_cur[tid] = R->cur;
-          }
+  const int cnt = min(*A.unit_cnt, A.unit_cap);
+  for (int u = blockIdx.x; u < cnt; u += gridDim.x) {
+    const int4 w = A.units[u];
+    const int r = w.x, kind = w.y & 0xFF, mode = w.y >> 8;
+    RepDev* R = &A.rep[r];
+    if (kind == U_OBS) {
+      replica_obs(A, R, w.w, red);
+    } else if (kind == U_ENERGY) {
+      replica_energy(A, R, w.w, red);
+    } else if (kind == U_BUILD) {
+      const int n = R->n, nsl = (n + kSliceBeads - 1) / kSliceBeads;
+      const int b0 = w.z * kSliceBeads, b1 = min(n, b0 + kSliceBeads);
+      build_lists(A, r, w.w, mode, b0, b1, B, dyn);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&A.slice_done[r], 1) == nsl - 1;
+      }
+      __syncthreads();
+      if (s_last) {
+        __threadfence();
+        if (threadIdx.x == 0) {
+          R->builds += 1;
+          R->rebuild = 0;
         }
+        if (R->en_after) replica_energy(A, R, R->cur, red);
       }
     }
     __syncthreads();
-    for (int q = 0; q < 64 && chunk + q < per; q++) {
-      if (!(s_obs[q] | s_build[q] | s_en[q])) continue;
-      const int k = blockIdx.x + (chunk + q) * gridDim.x;
-      RepDev* R = &A.rep[rep_ids[k]];
-      if (s_obs[q]) replica_obs(A, R, s_prev[q], red);
-      if (s_build[q]) { build_lists(A, rep_ids[k], s_prev[q], s_mode[q], B, dyn); __syncthreads(); }
-      if (s_en[q]) replica_energy(A, R, s_cur[q], red);
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(A.unit_exit, 1) == (int)gridDim.x - 1) {
+      *A.unit_cnt = 0;
+      *A.unit_exit = 0;
     }
-    __syncthreads();
   }
 }
 
@@ -645,9 +746,8 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
         }
       }
       if (upd) {
-        const double rc2 = c_ff.rc2_pl[ti][tj];
-        const bool plb = within(d2, (float)rc2, margin, [&] {
-          return exact_d2(Xc, cap, g, (long long)C.off + j) < rc2;
+        const bool plb = within(d2, c_ff.rc2_pl_f[ti][tj], margin, [&] {
+          return exact_d2(Xc, cap, g, (long long)C.off + j) < c_ff.rc2_pl[ti][tj];
         });
         if (plb != ((e & (int)kPL) != 0)) A.nl[row + k] = e ^ (int)kPL;
       }
@@ -988,8 +1088,8 @@ __global__ void k_pairlist(DevArrays A, int r, int off, int n) {
     const float d2 = dx * dx + dy * dy + dz * dz;
     const int tj = (int)hj.w;
     const double rc2 = c_ff.rc2_pl[ti][tj];
-    const bool plb =
-        within(d2, (float)rc2, kScreenMargin, [&] { return exact_d2(X, cap, gi, off + j) < rc2; });
+    const bool plb = within(d2, c_ff.rc2_pl_f[ti][tj], kScreenMargin,
+                            [&] { return exact_d2(X, cap, gi, off + j) < rc2; });
     A.nl[row + k] = (e & ~(int)kPL) | (plb ? (int)kPL : 0);
   }
 }
@@ -1045,7 +1145,7 @@ static cudaError_t optin(K kernel, int optin_bytes) {
 
 cudaError_t init_kernels(int optin_bytes) {
   cudaError_t e;
-  if ((e = optin(k_prologue, optin_bytes)) != cudaSuccess) return e;
+  if ((e = optin(k_build, optin_bytes)) != cudaSuccess) return e;
   if ((e = optin(k_step<1>, optin_bytes)) != cudaSuccess) return e;
   if ((e = optin(k_step<2>, optin_bytes)) != cudaSuccess) return e;
   if ((e = optin(k_step<4>, optin_bytes)) != cudaSuccess) return e;
@@ -1057,9 +1157,12 @@ cudaError_t init_kernels(int optin_bytes) {
 cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, int max_n,
                             int force_build, int build_mode, int grid, cudaStream_t s) {
   if (nrep <= 0) return cudaSuccess;
-  size_t dyn = build_dyn_smem(max_n);
-  if (grid <= 0 || grid > nrep) grid = nrep;
-  k_prologue<<<grid, kBuildThreads, dyn, s>>>(A, rep_ids, nrep, force_build, build_mode);
+  k_decide<<<(nrep + 127) / 128, 128, 0, s>>>(A, rep_ids, nrep, force_build, build_mode);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const size_t dyn = build_dyn_smem(max_n);
+  if (grid <= 0) grid = 1;
+  k_build<<<grid, kBuildThreads, dyn, s>>>(A);
   return cudaGetLastError();
 }
 

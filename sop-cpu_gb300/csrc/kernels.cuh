@@ -30,7 +30,14 @@ struct DevArrays {
   unsigned long long* pairs_out;  // export buffer (i<<32|j)
   int* pairs_cnt;
   int* err;           // engine-wide error word (bounded waits that gave up)
+  int4* units;        // per-step work queue (builds in slices, energies, observables)
+  int* unit_cnt;      // units queued this step
+  int* unit_exit;     // k_build CTAs finished (the last one resets the queue)
+  int* slice_done;    // per replica: build slices finished this step
+  int unit_cap;
 };
+
+constexpr int kSliceBeads = 128;      // beads per list-build work unit
 
 // Work item of the step kernel: beads [b0,b1) of replica r; staged = the
 // replica's positions fit in shared memory.

@@ -46,6 +46,7 @@ struct RepDev {
   int nat_base, bnd_base, ang_base, exc_base;  // entry bases
   // configuration
   int mode;                // SOP_LIST_*
+  int type_mask;           // bit t set when bead type t occurs in the replica
   int terms;               // SOP_TERM_* mask
   int prec;                // SOP_PREC_*
   int nnlup, nup;
@@ -76,6 +77,7 @@ struct RepDev {
   int rebuild;             // rebuild requested (SKIN displacement or host)
   int out;                 // this step is an output step
   int obs_pending;         // observables of the last output step still due
+  int en_after;            // energies due after this step's list build
   int running;             // a run window is open
   int active;
   int status;              // SOP_ST_* bits
@@ -101,6 +103,7 @@ struct FFTables {
   float fcr[kMaxTypes][kMaxTypes];   // force_coeff_rep as float
   float s2[kMaxTypes][kMaxTypes];    // sigma^2 as float
   double rc2_pl[kMaxTypes][kMaxTypes];   // (2.5 sigma)^2 in FP64, as sop.cpp:539-541
+  float rc2_pl_f[kMaxTypes][kMaxTypes];  // the same rounded to float, for the screen
   double rc2_nl[kMaxTypes][kMaxTypes];   // (3.2 sigma)^2 in FP64, as neighbor_list.cpp:97-100
 };
 

@@ -72,6 +72,7 @@ class EngineConfig(C.Structure):
         ("device", C.c_int), ("max_beads", C.c_int), ("max_replicas", C.c_int),
         ("max_list_entries", C.c_int64), ("block_threads", C.c_int),
         ("lanes_per_bead", C.c_int), ("graph_steps", C.c_int),
+        ("stage_limit", C.c_int), ("chunk_beads", C.c_int),
     ]
 
 
@@ -111,6 +112,7 @@ _PROTOS = {
     "sop_replica_set_state": (C.c_int, [VP, C.c_int, DP, DP]),
     "sop_replica_status": (C.c_int, [VP, C.c_int, IP, C.POINTER(C.c_int64)]),
     "sop_replica_count": (C.c_int, [VP, IP]),
+    "sop_replica_info": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int64)]),
     "sop_update_neighbor_list": (C.c_int, [VP, C.c_int]),
     "sop_update_cell_list": (C.c_int, [VP, C.c_int]),
     "sop_update_pair_list": (C.c_int, [VP, C.c_int]),

@@ -152,6 +152,12 @@ class Engine:
         L.check(L.lib().sop_replica_status(self.h, r, C.byref(st), C.byref(steps)), "sop_replica_status")
         return st.value, steps.value
 
+    def info(self, r: int) -> dict:
+        o = (C.c_int64 * 8)()
+        L.check(L.lib().sop_replica_info(self.h, r, o), "sop_replica_info")
+        keys = ("nbead", "L", "max_row", "builds", "t", "status", "natives", "offset")
+        return dict(zip(keys, list(o)))
+
     # -- reference-named operations
     def neighbor_list(self, r: int):
         L.check(L.lib().sop_update_neighbor_list(self.h, r), "sop_update_neighbor_list")
