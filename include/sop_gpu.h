@@ -234,6 +234,33 @@ int sop_synth_chain(uint64_t seed, int nbead, int compact_steps, double* xyz);
 /* nchain chains of chain_len beads packed into one globule. */
 int sop_synth_globule(uint64_t seed, int nchain, int chain_len, int compact_steps, double* xyz);
 
+/* ---- neighbor list without allocation ---------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory: code capturing a CUDA graph (cudaMalloc cannot be captured) and
+ * hosts whose device memory belongs to their own pool.  Every input and
+ * output is a device pointer owned by the caller; the only other memory used
+ * is a fixed static scratch array in the library (about 0.6 MB, held on each
+ * GPU that loads the library until exit), sized for SOP_NOALLOC_MAX_BEADS.
+ *   xyz      3*nbead doubles, x y z per bead (unc_pos)
+ *   bead_type, chain   nbead ints each, or NULL (all type 1, one chain)
+ *   nat_ptr, nat_idx   natives in CSR form (nat_ptr[nbead+1], partners of
+ *                      bead i in nat_idx[nat_ptr[i]..nat_ptr[i+1]), sorted),
+ *                      both listed per bead, or NULL for none
+ *   pairs    2*cap ints: 1-based (i, j), i < j, in no particular order
+ *   count    1 int: number of pairs found (only the first cap are written)
+ *   stream   a cudaStream_t, or NULL for the default stream
+ * Result: the non-native neighbor list of neighbor_list.cpp:70-116 -- pairs
+ * on different chains or |i-j| > 2 apart, not native, d^2 < (3.2 sigma)^2 in
+ * FP64 -- as the set sop_update_neighbor_list + sop_get_pair_list(which=1)
+ * give.  nbead > SOP_NOALLOC_MAX_BEADS returns SOP_ERR_UNSUPPORTED.  The
+ * first call on a device looks up the scratch address there; make it before
+ * any stream capture.  Calls share the scratch: calls that overlap on the GPU
+ * (different streams, or devices sharing it) race and must be ordered. */
+#define SOP_NOALLOC_MAX_BEADS 16384
+int sop_neighbor_list_noalloc(const double* xyz, int nbead, const int* bead_type, const int* chain,
+                              const int* nat_ptr, const int* nat_idx, int* pairs, int cap,
+                              int* count, void* stream);
+
 /* ---- host-side numerics self-checks (no GPU needed) ------------------------------- */
 /* split a double into the (hi, lo) float pair the engine stages */
 void sop_selftest_split(double x, float* hi, float* lo);

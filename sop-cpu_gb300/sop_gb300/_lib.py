@@ -136,6 +136,8 @@ _PROTOS = {
     "sop_server_stats": (C.c_int, [VP, C.POINTER(C.c_int64), IP, IP]),
     "sop_synth_chain": (C.c_int, [C.c_uint64, C.c_int, C.c_int, DP]),
     "sop_synth_globule": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.c_int, DP]),
+    "sop_neighbor_list_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "sop_selftest_split": (None, [C.c_double, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "sop_selftest_philox": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                    C.POINTER(C.c_uint32)]),
