@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--skin", type=float, default=2.0)
     ap.add_argument("--plain-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-steps", default="100,10000", help="log-uniform step-count range")
+    ap.add_argument("--serve-chunk", type=int, default=100)
     return ap.parse_args()
 
 
@@ -194,6 +198,102 @@ def algorithmic_bytes(eng, ids, systems):
     return tot
 
 
+PN_PER_KCAL_MOL_A = 69.48
+
+
+def serve_stream(args, rank):
+    """The serving stream: Poisson arrivals at --serve-rate of seeded chains
+    (N log-uniform 30-5000 from a pre-generated pool, steps log-uniform in
+    --serve-steps, T 0.4-0.9, constant pulling force 0-15 pN on the termini)
+    into the continuous-batching server for --serve-seconds."""
+    from sop_gb300 import _lib as L
+    from sop_gb300 import systems as S
+    from sop_gb300.engine import make_params
+    from sop_gb300.server import Server
+    rng = np.random.default_rng(4000 + 100000 * rank)
+    pool_sizes = np.unique(S.loguniform_sizes(4100 + rank, 48, 30, 5000))
+    xyzs = L.synth_many([(41000 + k, int(n)) for k, n in enumerate(pool_sizes)])
+    pool = [S.system_from_xyz(x) for x in xyzs]
+    lo, hi = (float(v) for v in args.serve_steps.split(","))
+    nreq = max(1, int(args.serve_rate * args.serve_seconds))
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, nreq))
+    target = np.exp(rng.uniform(math.log(30), math.log(5000), nreq))
+    pick = np.abs(np.log(pool_sizes)[None, :] - np.log(target)[:, None]).argmin(1)
+    steps = np.exp(rng.uniform(math.log(lo), math.log(hi), nreq)).round().astype(int)
+    temps = rng.uniform(0.4, 0.9, nreq)
+    pulls = rng.uniform(0.0, 15.0, nreq) / PN_PER_KCAL_MOL_A
+    params = [make_params(workload_script(), T=float(temps[k]), seed=90_000 + k,
+                          list_mode=args.list_mode, skin=args.skin, pull_force=float(pulls[k]))
+              for k in range(nreq)]
+    srv = Server(0, max_active=2048, chunk_steps=args.serve_chunk, max_beads=1 << 21,
+                 max_replicas=2100, max_list_entries=(1 << 21) * 96)
+    # warm-up requests, not timed
+    for k in range(8):
+        srv.submit(pool[k % len(pool)], 200, params[k])
+    while srv.pump():
+        pass
+    srv.poll()
+    t_start = srv.clock()
+    done, nxt, pending = [], 0, 0
+    while nxt < nreq or pending:
+        now = srv.clock() - t_start
+        while nxt < nreq and arrivals[nxt] <= now:
+            srv.submit(pool[pick[nxt]], int(steps[nxt]), params[nxt])
+            nxt += 1
+        pending = srv.pump()
+        done += srv.poll()
+        if pending == 0 and nxt < nreq:
+            time.sleep(max(0.0, min(0.005, arrivals[nxt] - (srv.clock() - t_start))))
+    done += srv.poll()
+    srv.close()
+    lat = np.array([r["finish"] - r["submit"] for r in done])
+    svc = np.array([r["finish"] - r["start"] for r in done])
+    work = sum(r["nbead"] * r["steps"] for r in done)
+    span = max(r["finish"] for r in done) - t_start
+    offered = float(np.sum(pool_sizes[pick] * steps)) / float(arrivals[-1])
+    return {"value": work / span, "unit": UNIT, "requests": len(done), "window_s": float(arrivals[-1]),
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "p50_service_s": float(np.percentile(svc, 50)), "p99_service_s": float(np.percentile(svc, 99)),
+            "offered_bead_steps_per_s": offered,
+            "errors": int(sum(1 for r in done if r["status"] or r["replica_status"])),
+            "stream": "Poisson %.0f req/s, N log-uniform 30-5000 (pool of %d seeded chains), steps "
+                      "log-uniform %g-%g (the 1e4-1e6 of the serving config scaled by 1/100 so requests "
+                      "complete inside the window), T 0.4-0.9, pull 0-15 pN"
+                      % (args.serve_rate, len(pool), lo, hi)}
+
+
+def force_check(eng, ids, systems, count=4):
+    """Force error of sampled replicas against the CPU oracle at their current
+    state (random term off on both sides): max normwise relative error."""
+    from oracle import oracle as O
+    from sop_gb300 import _lib as L
+    order = np.argsort([s.nbead for s in systems])
+    pick = order[np.linspace(0, len(order) - 1, count).round().astype(int)]
+    worst = 0.0
+    for k in pick:
+        r, s = ids[k], systems[k]
+        p = eng.params(r)
+        p.force_terms = L.TERM_FENE | L.TERM_ANGLE | L.TERM_VDW
+        eng.set_params(r, p)
+        eng.neighbor_list(r)
+        eng.pair_list(r)
+        f = eng.force(r)
+        _, x, _ = eng.state(r)
+        port = O.Port()
+        port.set_system(s)
+        for _, key, v in workload_script():
+            port.command(key, v)
+        port.set_coords(0, x)
+        port.set_coords(1, x)
+        port.set_force_terms(0, 1, 1, 1)
+        port.neighbor_list()
+        port.pair_list()
+        port.force_eval()
+        fr = port.coords(3)
+        worst = max(worst, float(np.linalg.norm(f - fr) / np.linalg.norm(fr)))
+    return worst
+
+
 def flush_l2():
     import torch
     buf = getattr(flush_l2, "buf", None)
@@ -269,6 +369,9 @@ def run_gb300(args):
         eng.run_plain(r, args.plain_steps)
         plain_ms += eng.timing()[0]
     plain = beads * args.plain_steps / (plain_ms / 1e3)
+    ferr = force_check(eng, ids, systems)
+    eng.close()
+    served = serve_stream(args, rank) if args.serve_seconds > 0 else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -285,6 +388,8 @@ def run_gb300(args):
         "gpu_launches": int(launches),
         "plain_gpu_path": {"value": plain, "unit": UNIT, "steps": args.plain_steps,
                            "batched_over_plain": value / plain},
+        "served": served,
+        "force_rel_err": ferr,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                      "kernel": "k_step (fused force + Langevin)", "kernel_ms": step_ms,
@@ -293,7 +398,6 @@ def run_gb300(args):
     }
     if rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(systems, temps, args.cpu_seconds)
-    eng.close()
     if rank == 0:
         print(json.dumps(line))
 

@@ -178,6 +178,13 @@ int sop_run_plain(sop_engine* e, int replica, int64_t nsteps);
 /* All active replicas, packed into one persistent kernel per step, with
  * per-replica rebuilds, the step loop captured in CUDA graphs. */
 int sop_run(sop_engine* e, int64_t nsteps);
+/* Per-replica run windows for continuous batching: sop_replica_start opens
+ * a window of nsteps for one replica (restart semantics: its first step
+ * re-evaluates the force at the stored state); sop_run_chunk advances every
+ * open window by up to `steps` batched steps; replicas whose window closed
+ * during the chunk are returned in finished[0..*nfinished) (cap entries). */
+int sop_replica_start(sop_engine* e, int replica, int64_t nsteps);
+int sop_run_chunk(sop_engine* e, int64_t steps, int* finished, int cap, int* nfinished);
 /* End-to-end call with HOST buffers (restart semantics, sop.cpp:132-147):
  * load unc_pos/vel of every active replica (packed in replica-id order,
  * 3*nbead each), evaluate the initial force, run nsteps, write them back. */
@@ -224,7 +231,7 @@ int sop_server_submit(sop_server* s, const sop_system_desc* d, int64_t nsteps, i
 int sop_server_pump(sop_server* s, int* pending);
 /* completed requests since the last call */
 int sop_server_poll(sop_server* s, sop_request_result* out, int cap, int* n);
-/* final state of a completed request (unc_pos 3*nbead); valid until polled twice */
+/* seconds since the server was created (the clock of submit/start/finish) */
 int sop_server_clock(sop_server* s, double* now_s);
 int sop_server_stats(sop_server* s, int64_t* bead_steps, int* active, int* queued);
 

@@ -186,10 +186,10 @@ extern "C" void sop_engine_config_default(sop_engine_config* c) {
   c->max_replicas = 4096;
   c->max_list_entries = (int64_t)(1 << 21) * 64;
   c->block_threads = 256;
-  c->lanes_per_bead = 4;
+  c->lanes_per_bead = 2;
   c->graph_steps = 20;
-  c->stage_limit = kStageMax;
-  c->chunk_beads = 256;
+  c->stage_limit = 2048;
+  c->chunk_beads = 128;
 }
 
 // ---- engine lifetime ------------------------------------------------------------
@@ -270,6 +270,10 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   A.unit_exit = A.unit_cnt + 1;
   CK(dalloc(&A.slice_done, cfg.max_replicas));
   CK(cudaMemsetAsync(A.unit_cnt, 0, 2 * sizeof(int), e->stream));
+  A.done_cap = cfg.max_replicas;
+  CK(dalloc(&A.done_list, A.done_cap));
+  CK(dalloc(&A.done_cnt, 1));
+  CK(cudaMemsetAsync(A.done_cnt, 0, sizeof(int), e->stream));
   CK(cudaMemsetAsync(A.slice_done, 0, sizeof(int) * cfg.max_replicas, e->stream));
   CK(cudaMemsetAsync(A.rep, 0, sizeof(RepDev) * cfg.max_replicas, e->stream));
   CK(dalloc(&e->d_ids, cfg.max_replicas + 4));
@@ -286,6 +290,18 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   upload_tables(tables(), e->stream);
   CK(cudaGetLastError());
   CK(init_kernels((int)e->prop.sharedMemPerBlockOptin));
+  CK(dalloc(&e->d_counts, 2));
+  CK(cudaMemsetAsync(e->d_counts, 0, 2 * sizeof(int), e->stream));
+  CK(dalloc(&e->d_pack_xyz, 3 * cap));
+  CK(dalloc(&e->d_pack_vel, 3 * cap));
+  CK(dalloc(&e->d_pack_ids, cfg.max_replicas));
+  CK(dalloc(&e->d_pack_off, cfg.max_replicas));
+  // fixed launch shapes of the batched step (so captured graphs stay valid):
+  // persistent step CTAs as many as fit, staging sized by the stage limit
+  e->max_staged = cfg.stage_limit > 0 ? cfg.stage_limit : 0;
+  e->step_grid = step_blocks_per_sm(cfg.lanes_per_bead, cfg.block_threads, e->max_staged) *
+                 e->prop.multiProcessorCount;
+  e->pro_grid = 2 * e->prop.multiProcessorCount;  // k_build CTAs over the unit queue
   for (int k = 0; k < 4; k++) CK(cudaEventCreate(&e->ev[k]));
   CK(cudaStreamSynchronize(e->stream));
   *out = e.release();
@@ -301,7 +317,8 @@ extern "C" int sop_engine_destroy(sop_engine* e) {
   void* ptrs[] = {A.X[0], A.X[1], A.stage[0], A.stage[1], A.incr, A.vel, A.force, A.xb, A.topo,
                   A.exc_rng, A.nl_cnt, A.nl, A.nat, A.nat_r0, A.bnd, A.bnd_r0, A.ang, A.exc,
                   A.rep, A.pairs_out, A.pairs_cnt, A.err, A.units, A.unit_cnt, A.slice_done,
-                  e->d_ids, e->d_items};
+                  A.done_list, A.done_cnt, e->d_ids, e->d_items, e->d_counts, e->d_pack_xyz,
+                  e->d_pack_vel, e->d_pack_ids, e->d_pack_off};
   for (void* p : ptrs) cudaFree(p);
   if (e->h_rep) cudaFreeHost(e->h_rep);
   for (int k = 0; k < 4; k++) if (e->ev[k]) cudaEventDestroy(e->ev[k]);
@@ -376,16 +393,31 @@ static int max_candidates(const sop_system_desc* d, const std::vector<int>& type
     }
   double edge = mode == SOP_LIST_CELL ? d->params.lcell : rl;
   if (edge <= 0) return n;
-  std::unordered_map<long long, std::vector<int>> grid;
-  auto key = [](long long a, long long b, long long c) {
-    return ((a + (1 << 20)) << 42) ^ ((b + (1 << 20)) << 21) ^ (c + (1 << 20));
-  };
-  std::vector<long long> cx(n), cy(n), cz(n);
+  // flat cell grid over the bounding box (counting sort), widened if huge
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int i = 0; i < n; i++)
+    for (int c = 0; c < 3; c++) {
+      lo[c] = std::min(lo[c], x[3 * i + c]);
+      hi[c] = std::max(hi[c], x[3 * i + c]);
+    }
+  long long dim[3];
+  for (;;) {
+    for (int c = 0; c < 3; c++) dim[c] = (long long)((hi[c] - lo[c]) / edge) + 1;
+    if (dim[0] * dim[1] * dim[2] <= (1LL << 22)) break;
+    edge *= 1.5;
+  }
+  const long long ncell = dim[0] * dim[1] * dim[2];
+  std::vector<int> cx(n), cy(n), cz(n), cstart(ncell + 1, 0), sorted(n);
   for (int i = 0; i < n; i++) {
-    cx[i] = (long long)std::floor(x[3 * i] / edge);
-    cy[i] = (long long)std::floor(x[3 * i + 1] / edge);
-    cz[i] = (long long)std::floor(x[3 * i + 2] / edge);
-    grid[key(cx[i], cy[i], cz[i])].push_back(i);
+    cx[i] = std::min<long long>((long long)((x[3 * i] - lo[0]) / edge), dim[0] - 1);
+    cy[i] = std::min<long long>((long long)((x[3 * i + 1] - lo[1]) / edge), dim[1] - 1);
+    cz[i] = std::min<long long>((long long)((x[3 * i + 2] - lo[2]) / edge), dim[2] - 1);
+    cstart[cx[i] + dim[0] * (cy[i] + dim[1] * cz[i]) + 1]++;
+  }
+  for (long long c = 0; c < ncell; c++) cstart[c + 1] += cstart[c];
+  {
+    std::vector<int> fill(cstart.begin(), cstart.end() - 1);
+    for (int i = 0; i < n; i++) sorted[fill[cx[i] + dim[0] * (cy[i] + dim[1] * cz[i])]++] = i;
   }
   int best = 0;
   for (int i = 0; i < n; i++) {
@@ -393,9 +425,11 @@ static int max_candidates(const sop_system_desc* d, const std::vector<int>& type
     for (int a = -1; a <= 1; a++)
       for (int b = -1; b <= 1; b++)
         for (int c = -1; c <= 1; c++) {
-          auto it = grid.find(key(cx[i] + a, cy[i] + b, cz[i] + c));
-          if (it == grid.end()) continue;
-          for (int j : it->second) {
+          const long long xx = cx[i] + a, yy = cy[i] + b, zz = cz[i] + c;
+          if (xx < 0 || yy < 0 || zz < 0 || xx >= dim[0] || yy >= dim[1] || zz >= dim[2]) continue;
+          const long long cc = xx + dim[0] * (yy + dim[1] * zz);
+          for (int s = cstart[cc]; s < cstart[cc + 1]; s++) {
+            const int j = sorted[s];
             if (j == i) continue;
             if (chain[i] == chain[j] && std::abs(i - j) <= 2) continue;
             if (mode == SOP_LIST_CELL) { cnt++; continue; }
@@ -622,9 +656,9 @@ int sop::build_now(sop_engine* e, int r, int mode) {
   CK(cudaMemcpyAsync(e->d_ids + scratch_id(e, 0), &id, sizeof(int), cudaMemcpyHostToDevice,
                      e->stream));
   const int nsl = (R.n + kSliceBeads - 1) / kSliceBeads;
-  CK(launch_prologue(e->A, e->d_ids + scratch_id(e, 0), 1, R.n, 1, mode,
+  CK(launch_prologue(e->A, e->d_ids + scratch_id(e, 0), 1, nullptr, R.n, 1, mode,
                      std::min(nsl, 2 * e->prop.multiProcessorCount), e->stream));
-  e->launches++;
+  e->launches += 2;
   CK(cudaStreamSynchronize(e->stream));
   return SOP_OK;
 }
@@ -715,6 +749,30 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
   // set-up of underdamped_ctrl (sop.cpp:117-125): lists at the initial positions
   rc = build_now(e, slot, d->params.list_mode);
   if (rc) return rc;
+  // rows sized from a host estimate; if the build found a longer row, grow
+  // the replica's list range to fit it with room to spare and build again
+  for (int attempt = 0; attempt < 3; attempt++) {
+    RepDev got;
+    rc = get_rep(e, slot, &got);
+    if (rc) return rc;
+    if (!(got.status & SOP_ST_LIST_OVERFLOW)) break;
+    const int L2 = ((got.max_row + got.max_row / 2 + 32) + 7) / 8 * 8;
+    long long nlb2;
+    e->lists.release(R.nl_base, (long long)n * R.L);
+    if (!e->lists.alloc((long long)n * L2, 8, &nlb2)) {
+      sop_replica_remove(e, slot);
+      return SOP_ERR_FULL;
+    }
+    R.nl_base = nlb2;
+    R.L = L2;
+    got.nl_base = nlb2;
+    got.L = L2;
+    got.status &= ~SOP_ST_LIST_OVERFLOW;
+    rc = put_rep(e, slot, got);
+    if (rc) return rc;
+    rc = build_now(e, slot, d->params.list_mode);
+    if (rc) return rc;
+  }
   e->layout_dirty = true;
   *replica = slot;
   return SOP_OK;
@@ -837,7 +895,9 @@ extern "C" int sop_replica_set_state(sop_engine* e, int r, const double* unc_pos
   if (rc) return rc;
   rc = upload_velocities(e, r, vel);
   if (rc) return rc;
-  return SOP_OK;
+  // lists for the new positions (the reference builds them before loading a
+  // restart, sop.cpp:119-136, and runs on stale lists until the next rebuild)
+  return build_now(e, r, e->reps[r].params.list_mode);
 }
 
 extern "C" int sop_replica_status(sop_engine* e, int r, int* status, int64_t* steps) {
@@ -890,35 +950,49 @@ int sop::refresh_layout(sop_engine* e) {
   std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return e->reps[a].n > e->reps[b].n; });
   e->active = ids;
   e->max_n = 0;
-  e->max_staged = 0;
   e->items.clear();
   for (int r : ids) {
     const Replica& R = e->reps[r];
     e->max_n = std::max(e->max_n, R.n);
     std::vector<StepItem> it = replica_items(e, r);
-    if (it[0].staged) e->max_staged = std::max(e->max_staged, R.n);
     e->items.insert(e->items.end(), it.begin(), it.end());
   }
-  if ((long long)e->items.size() > e->items_cap) return SOP_ERR_FULL;
+  if ((long long)e->items.size() + 64 > e->items_cap) return SOP_ERR_FULL;
+  // the kernels read the counts from device memory, so a captured graph stays
+  // valid; only a new shared-memory size class for k_build needs a recapture
+  const int counts[2] = {(int)ids.size(), (int)e->items.size()};
   if (!ids.empty()) CK(h2d(e->d_ids, ids.data(), ids.size(), e->stream));
   if (!e->items.empty()) CK(h2d(e->d_items, e->items.data(), e->items.size(), e->stream));
-  CK(cudaStreamSynchronize(e->stream));
-  // persistent grid: as many CTAs as fit at once, at most one per item
-  const int per_sm = step_blocks_per_sm(e->cfg.lanes_per_bead, e->cfg.block_threads, e->max_staged);
-  e->step_grid = std::max(1, std::min((int)e->items.size(), per_sm * e->prop.multiProcessorCount));
-  e->pro_grid = e->prop.multiProcessorCount * 2;  // k_build CTAs over the unit queue
+  CK(h2d(e->d_counts, counts, 2, e->stream));
+  int bucket = 1024;
+  while (bucket < e->max_n) bucket <<= 1;
+  bucket = std::min(bucket, kBuildMax);
+  if (bucket != e->build_bucket) {
+    e->build_bucket = bucket;
+    e->graph_valid = false;
+  }
   e->layout_dirty = false;
-  e->graph_valid = false;
   return SOP_OK;
 }
 
-// One batched step: prologue (+ builds, energies, observables) then the step kernel.
+// One step over given ids / items with host counts (single-replica paths).
 int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items,
                       int nitems, int max_n, int max_staged, int step_grid, int pro_grid) {
-  CK(launch_prologue(e->A, d_ids, nrep, max_n, 0, 0, pro_grid, e->stream));
-  CK(launch_step(e->A, d_items, nitems, max_staged, e->cfg.lanes_per_bead, e->cfg.block_threads,
-                 step_grid, e->stream));
-  e->launches += 2;
+  CK(launch_prologue(e->A, d_ids, nrep, nullptr, max_n, 0, 0, pro_grid, e->stream));
+  CK(launch_step(e->A, d_items, nitems, nullptr, max_staged, e->cfg.lanes_per_bead,
+                 e->cfg.block_threads, step_grid, e->stream));
+  e->launches += 3;
+  return SOP_OK;
+}
+
+// One batched step: k_decide, k_build (builds, energies, observables), k_step,
+// sized by the engine's fixed grids and the device-resident counts.
+int sop::enqueue_batched_step(sop_engine* e) {
+  CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, e->build_bucket, 0, 0,
+                     e->pro_grid, e->stream));
+  CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, e->max_staged,
+                 e->cfg.lanes_per_bead, e->cfg.block_threads, e->step_grid, e->stream));
+  e->launches += 3;
   return SOP_OK;
 }
 
@@ -993,8 +1067,7 @@ static int capture_graph(sop_engine* e) {
   CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
   int64_t before = e->launches;
   for (int s = 0; s < e->cfg.graph_steps; s++) {
-    int rc = enqueue_step(e, e->d_ids, (int)e->active.size(), e->d_items, (int)e->items.size(),
-                          e->max_n, e->max_staged, e->step_grid, e->pro_grid);
+    int rc = enqueue_batched_step(e);
     if (rc) { cudaStreamEndCapture(e->stream, &g); return rc; }
   }
   e->launches = before;  // counted when replayed
@@ -1021,11 +1094,10 @@ int sop::run_batched(sop_engine* e, int64_t nsteps, bool timed) {
   const int64_t full = iters / S;
   for (int64_t k = 0; k < full; k++) {
     CK(cudaGraphLaunch(e->graph_exec, e->stream));
-    e->launches += 2 * S;
+    e->launches += 3 * S;
   }
   for (int64_t k = full * S; k < iters; k++) {
-    rc = enqueue_step(e, e->d_ids, nrep, e->d_items, (int)e->items.size(), e->max_n, e->max_staged,
-                      e->step_grid, e->pro_grid);
+    rc = enqueue_batched_step(e);
     if (rc) return rc;
   }
   CK(launch_observables(e->A, e->d_ids, nrep, e->stream));
@@ -1038,6 +1110,52 @@ int sop::run_batched(sop_engine* e, int64_t nsteps, bool timed) {
     e->last_total_ms = ms;
   }
   e->last_step_launches = iters;
+  return check_errors(e);
+}
+
+extern "C" int sop_replica_start(sop_engine* e, int r, int64_t nsteps) {
+  if (!e || !live(e, r) || nsteps < 1) return SOP_ERR_ARG;
+  CK(cudaSetDevice(e->cfg.device));
+  const int slot = scratch_id(e, 2);
+  CK(cudaMemcpyAsync(e->d_ids + slot, &r, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  k_begin<<<1, 32, 0, e->stream>>>(e->A.rep, e->d_ids + slot, 1, nsteps);
+  e->launches++;
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(e->stream));  // the id slot is reused by the next call
+  return SOP_OK;
+}
+
+extern "C" int sop_run_chunk(sop_engine* e, int64_t steps, int* finished, int cap, int* nfinished) {
+  if (!e || steps < 0 || (cap > 0 && !finished)) return SOP_ERR_ARG;
+  CK(cudaSetDevice(e->cfg.device));
+  int rc = refresh_layout(e);
+  if (rc) return rc;
+  if (nfinished) *nfinished = 0;
+  if (e->active.empty() || steps == 0) return SOP_OK;
+  rc = capture_graph(e);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(e->A.done_cnt, 0, sizeof(int), e->stream));
+  CK(cudaEventRecord(e->ev[0], e->stream));
+  const int S = e->cfg.graph_steps;
+  for (int64_t k = 0; k < steps / S; k++) {
+    CK(cudaGraphLaunch(e->graph_exec, e->stream));
+    e->launches += 3 * S;
+  }
+  for (int64_t k = steps / S * S; k < steps; k++) {
+    rc = enqueue_batched_step(e);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(e->ev[1], e->stream));
+  int nd = 0;
+  CK(cudaMemcpyAsync(&nd, e->A.done_cnt, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]);
+  e->last_total_ms = ms;
+  nd = std::min(nd, e->A.done_cap);
+  if (nd > 0 && cap > 0)
+    CK(cudaMemcpy(finished, e->A.done_list, std::min(nd, cap) * sizeof(int), cudaMemcpyDeviceToHost));
+  if (nfinished) *nfinished = nd;
   return check_errors(e);
 }
 
@@ -1070,12 +1188,13 @@ extern "C" int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_ms,
   for (auto& x : ev) CK(cudaEventCreate(&x));
   for (int64_t s = 0; s < iters; s++) {
     CK(cudaEventRecord(ev[3 * s], e->stream));
-    CK(launch_prologue(e->A, e->d_ids, nrep, e->max_n, 0, 0, e->pro_grid, e->stream));
+    CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, e->build_bucket, 0, 0,
+                       e->pro_grid, e->stream));
     CK(cudaEventRecord(ev[3 * s + 1], e->stream));
-    CK(launch_step(e->A, e->d_items, (int)e->items.size(), e->max_staged, e->cfg.lanes_per_bead,
-                   e->cfg.block_threads, e->step_grid, e->stream));
+    CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, e->max_staged,
+                   e->cfg.lanes_per_bead, e->cfg.block_threads, e->step_grid, e->stream));
     CK(cudaEventRecord(ev[3 * s + 2], e->stream));
-    e->launches += 2;
+    e->launches += 3;
   }
   CK(cudaStreamSynchronize(e->stream));
   double ts = 0, tp = 0;
@@ -1098,25 +1217,38 @@ extern "C" int sop_run_host(sop_engine* e, const double* xyz_in, const double* v
   int rc = refresh_layout(e);
   if (rc) return rc;
   std::vector<int> ids;
+  std::vector<long long> poff;
+  long long total = 0;
   for (int r = 0; r < (int)e->reps.size(); r++)
-    if (e->reps[r].live) ids.push_back(r);
-  long long o = 0;
-  for (int r : ids) {
-    rc = upload_positions(e, r, xyz_in + o, 3);
-    if (rc) return rc;
-    rc = upload_velocities(e, r, vel_in ? vel_in + o : nullptr);
-    if (rc) return rc;
-    o += 3LL * e->reps[r].n;
-  }
+    if (e->reps[r].live) {
+      ids.push_back(r);
+      poff.push_back(total);
+      total += e->reps[r].n;
+    }
+  const int nrep = (int)ids.size();
+  if (nrep == 0) return SOP_OK;
+  // one copy in, scatter on the device, lists rebuilt at the new positions
+  CK(h2d(e->d_pack_ids, ids.data(), nrep, e->stream));
+  CK(h2d(e->d_pack_off, poff.data(), nrep, e->stream));
+  CK(h2d(e->d_pack_xyz, xyz_in, 3 * total, e->stream));
+  if (vel_in) CK(h2d(e->d_pack_vel, vel_in, 3 * total, e->stream));
+  CK(launch_scatter_state(e->A, e->d_pack_ids, nrep, e->d_pack_off, e->d_pack_xyz,
+                          vel_in ? e->d_pack_vel : nullptr, e->stream));
+  CK(launch_prologue(e->A, e->d_pack_ids, nrep, nullptr, e->max_n, 1, -1, e->pro_grid, e->stream));
+  e->launches += 3;
   rc = run_batched(e, nsteps, false);
   if (rc) return rc;
-  o = 0;
-  for (int r : ids) {
-    rc = sop_replica_get_state(e, r, nullptr, xyz_out ? xyz_out + o : nullptr,
-                               vel_out ? vel_out + o : nullptr);
-    if (rc) return rc;
-    o += 3LL * e->reps[r].n;
-  }
+  // gather on the device, one copy out
+  CK(launch_gather_state(e->A, e->d_pack_ids, nrep, e->d_pack_off, e->d_pack_xyz, e->d_pack_vel,
+                         e->stream));
+  e->launches++;
+  if (xyz_out)
+    CK(cudaMemcpyAsync(xyz_out, e->d_pack_xyz, 3 * total * sizeof(double), cudaMemcpyDeviceToHost,
+                       e->stream));
+  if (vel_out)
+    CK(cudaMemcpyAsync(vel_out, e->d_pack_vel, 3 * total * sizeof(double), cudaMemcpyDeviceToHost,
+                       e->stream));
+  CK(cudaStreamSynchronize(e->stream));
   return SOP_OK;
 }
 
@@ -1173,7 +1305,7 @@ static int run_phase(sop_engine* e, int r, int phase) {
   const long long item_slot = e->items_cap - (long long)items.size();
   CK(h2d(e->d_items + item_slot, items.data(), items.size(), e->stream));
   k_set_phase<<<1, 1, 0, e->stream>>>(e->A.rep, r, phase);
-  CK(launch_step(e->A, e->d_items + item_slot, (int)items.size(), staged ? R.n : 0,
+  CK(launch_step(e->A, e->d_items + item_slot, (int)items.size(), nullptr, staged ? R.n : 0,
                  e->cfg.lanes_per_bead, e->cfg.block_threads,
                  std::min((int)items.size(), 4 * e->prop.multiProcessorCount), e->stream));
   e->launches += 2;

@@ -66,6 +66,13 @@ struct sop_engine {
   std::vector<int> active;
   std::vector<sop::StepItem> items;
   int max_n = 0, max_staged = 0, step_grid = 1, pro_grid = 1;
+  int* d_counts = nullptr;          // {active replicas, work items}, read by the kernels
+  int build_bucket = 0;             // k_build shared-memory size class (beads)
+  // packed host-order state of sop_run_host (one copy each way)
+  double* d_pack_xyz = nullptr;
+  double* d_pack_vel = nullptr;
+  int* d_pack_ids = nullptr;
+  long long* d_pack_off = nullptr;
   bool layout_dirty = true;
   // CUDA graph of graph_steps batched steps
   cudaGraphExec_t graph_exec = nullptr;
@@ -87,6 +94,8 @@ int build_now(sop_engine* e, int r, int mode);
 int refresh_layout(sop_engine* e);
 int enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items, int nitems,
                  int max_n, int max_staged, int step_grid, int pro_grid);
+// one step of every active replica, sized only by device-resident counts
+int enqueue_batched_step(sop_engine* e);
 int run_batched(sop_engine* e, int64_t nsteps, bool timed);
 inline int scratch_id(const sop_engine* e, int k) { return e->cfg.max_replicas + k; }
 }  // namespace sop

@@ -546,18 +546,26 @@ __device__ __forceinline__ void push_units(const DevArrays& A, int r, int kind, 
 //   the list build from X_{t-1} in slices (sop.cpp:156-170: rebuild before the step),
 //   the energies of this output step at X_t with pair list PL_t (after the build,
 //   before the step kernel rewrites the pair-list bits).
-__global__ void k_decide(DevArrays A, const int* rep_ids, int nrep, int force_build, int build_mode) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nrep) return;
-  const int r = rep_ids[k];
+__device__ void decide_one(const DevArrays& A, int r, int force_build, int build_mode);
+
+// nrep comes from device memory when nrep_dev is set, so a captured graph
+// keeps working when replicas are admitted or retired.
+__global__ void k_decide(DevArrays A, const int* rep_ids, const int* nrep_dev, int nrep_host,
+                         int force_build, int build_mode) {
+  const int nrep = nrep_dev ? *nrep_dev : nrep_host;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nrep; k += gridDim.x * blockDim.x)
+    decide_one(A, rep_ids[k], force_build, build_mode);
+}
+
+__device__ void decide_one(const DevArrays& A, int r, int force_build, int build_mode) {
   RepDev* R = &A.rep[r];
   RepDev Q = *R;  // one pipelined copy; decide in registers, store back
   const int nsl = (Q.n + kSliceBeads - 1) / kSliceBeads;
-  if (force_build) {
+  if (force_build) {  // build_mode < 0: the replica's own list mode
     A.slice_done[r] = 0;
     R->max_row = 0;
     R->en_after = 0;
-    push_units(A, r, U_BUILD, build_mode, nsl, Q.cur);
+    push_units(A, r, U_BUILD, build_mode >= 0 ? build_mode : Q.mode, nsl, Q.cur);
     return;
   }
   if (Q.obs_pending) {
@@ -591,6 +599,8 @@ __global__ void k_decide(DevArrays A, const int* rep_ids, int nrep, int force_bu
   R->t_cur = Q.t;
   if (ph == PH_FINAL) {
     R->running = 0;
+    const int slot = atomicAdd(A.done_cnt, 1);
+    if (slot < A.done_cap) A.done_list[slot] = r;
   } else {
     R->t = Q.t + 1;
     Q.moved = 1;
@@ -856,7 +866,9 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
 }
 
 template <int G>
-__global__ void __launch_bounds__(256, 3) k_step(DevArrays A, const StepItem* items, int nitems) {
+__global__ void __launch_bounds__(256, 3) k_step(DevArrays A, const StepItem* items,
+                                                 const int* nitems_dev, int nitems_host) {
+  const int nitems = nitems_dev ? *nitems_dev : nitems_host;
   extern __shared__ __align__(128) float4 sst[];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ ItemCtx sC;
@@ -1094,6 +1106,60 @@ __global__ void k_pairlist(DevArrays A, int r, int off, int n) {
   }
 }
 
+// Packed host-order state (x y z per bead, replicas back to back at 3*poff[k])
+// into replica k's device arrays: both position buffers, the staged float
+// pairs, velocities, zero increments.  One CTA per replica.
+__global__ void k_scatter_state(DevArrays A, const int* ids, const long long* poff,
+                                const double* xyz, const double* vel) {
+  const RepDev* R = &A.rep[ids[blockIdx.x]];
+  const long long off = R->off, cap = A.cap, base = 3 * poff[blockIdx.x];
+  for (int i = threadIdx.x; i < R->n; i += blockDim.x) {
+    const long long g = off + i;
+    float h[3], l[3];
+    for (int c = 0; c < 3; c++) {
+      const double x = xyz[base + 3 * i + c];
+      A.X[0][c * cap + g] = x;
+      A.X[1][c * cap + g] = x;
+      split_double(x, h[c], l[c]);
+      A.vel[c * cap + g] = vel ? vel[base + 3 * i + c] : 0.0;
+      A.incr[c * cap + g] = 0.0f;
+    }
+    const float4 oh = A.stage[0][2 * g], ol = A.stage[0][2 * g + 1];  // keep type / chain
+    const float4 nh = make_float4(h[0], h[1], h[2], oh.w), nl = make_float4(l[0], l[1], l[2], ol.w);
+    A.stage[0][2 * g] = nh;
+    A.stage[1][2 * g] = nh;
+    A.stage[0][2 * g + 1] = nl;
+    A.stage[1][2 * g + 1] = nl;
+  }
+}
+
+// The reverse: current positions and velocities into the packed layout.
+__global__ void k_gather_state(DevArrays A, const int* ids, const long long* poff, double* xyz,
+                               double* vel) {
+  const RepDev* R = &A.rep[ids[blockIdx.x]];
+  const long long off = R->off, cap = A.cap, base = 3 * poff[blockIdx.x];
+  const double* X = A.X[R->cur];
+  for (int i = threadIdx.x; i < R->n; i += blockDim.x)
+    for (int c = 0; c < 3; c++) {
+      if (xyz) xyz[base + 3 * i + c] = X[c * cap + off + i];
+      if (vel) vel[base + 3 * i + c] = A.vel[c * cap + off + i];
+    }
+}
+
+cudaError_t launch_scatter_state(const DevArrays& A, const int* ids, int nrep, const long long* poff,
+                                 const double* xyz, const double* vel, cudaStream_t s) {
+  if (nrep <= 0) return cudaSuccess;
+  k_scatter_state<<<nrep, 256, 0, s>>>(A, ids, poff, xyz, vel);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_state(const DevArrays& A, const int* ids, int nrep, const long long* poff,
+                                double* xyz, double* vel, cudaStream_t s) {
+  if (nrep <= 0) return cudaSuccess;
+  k_gather_state<<<nrep, 256, 0, s>>>(A, ids, poff, xyz, vel);
+  return cudaGetLastError();
+}
+
 // which: 0 neighbor att, 1 neighbor rep, 2 pair att, 3 pair rep
 __global__ void k_export(DevArrays A, int r, int off, int n, int which, int capacity) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1154,10 +1220,11 @@ cudaError_t init_kernels(int optin_bytes) {
   return cudaSuccess;
 }
 
-cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, int max_n,
-                            int force_build, int build_mode, int grid, cudaStream_t s) {
+cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, const int* nrep_dev,
+                            int max_n, int force_build, int build_mode, int grid, cudaStream_t s) {
   if (nrep <= 0) return cudaSuccess;
-  k_decide<<<(nrep + 127) / 128, 128, 0, s>>>(A, rep_ids, nrep, force_build, build_mode);
+  const int dgrid = (nrep + 127) / 128;
+  k_decide<<<dgrid, 128, 0, s>>>(A, rep_ids, nrep_dev, nrep, force_build, build_mode);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const size_t dyn = build_dyn_smem(max_n);
@@ -1168,22 +1235,23 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, in
 
 template <int G>
 static cudaError_t launch_step_g(const DevArrays& A, const StepItem* items, int nitems,
-                                 size_t dyn, int threads, int grid, cudaStream_t s) {
-  k_step<G><<<grid, threads, dyn, s>>>(A, items, nitems);
+                                 const int* nitems_dev, size_t dyn, int threads, int grid,
+                                 cudaStream_t s) {
+  k_step<G><<<grid, threads, dyn, s>>>(A, items, nitems_dev, nitems);
   return cudaGetLastError();
 }
 
-cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, int max_staged,
-                        int lanes, int threads, int grid, cudaStream_t s) {
+cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
+                        int max_staged, int lanes, int threads, int grid, cudaStream_t s) {
   if (nitems <= 0) return cudaSuccess;
   size_t dyn = (size_t)max_staged * 32 + 128;
   if (grid <= 0) grid = nitems;
   switch (lanes) {
-    case 1: return launch_step_g<1>(A, items, nitems, dyn, threads, grid, s);
-    case 2: return launch_step_g<2>(A, items, nitems, dyn, threads, grid, s);
-    case 8: return launch_step_g<8>(A, items, nitems, dyn, threads, grid, s);
-    case 16: return launch_step_g<16>(A, items, nitems, dyn, threads, grid, s);
-    default: return launch_step_g<4>(A, items, nitems, dyn, threads, grid, s);
+    case 1: return launch_step_g<1>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
+    case 2: return launch_step_g<2>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
+    case 8: return launch_step_g<8>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
+    case 16: return launch_step_g<16>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
+    default: return launch_step_g<4>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
   }
 }
 

@@ -35,6 +35,9 @@ struct DevArrays {
   int* unit_exit;     // k_build CTAs finished (the last one resets the queue)
   int* slice_done;    // per replica: build slices finished this step
   int unit_cap;
+  int* done_list;     // replicas whose run window closed (final step taken)
+  int* done_cnt;
+  int done_cap;
 };
 
 constexpr int kSliceBeads = 128;      // beads per list-build work unit
@@ -57,13 +60,20 @@ cudaError_t init_kernels(int optin_bytes);
 // Prologue + list build: one persistent CTA group over `nrep` replica ids.
 // force_build: build for every listed replica from the CURRENT buffer
 // (reference-named list updates), else the step cadence decides.
-cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, int max_n,
-                            int force_build, int build_mode, int grid, cudaStream_t s);
-cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, int max_staged,
-                        int lanes, int threads, int grid, cudaStream_t s);
+// nrep / nitems: host counts (grid sizing); *_dev: the same counts in device
+// memory, read by the kernels when given (graphs survive layout changes).
+cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, const int* nrep_dev,
+                            int max_n, int force_build, int build_mode, int grid, cudaStream_t s);
+cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
+                        int max_staged, int lanes, int threads, int grid, cudaStream_t s);
 cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s);
 cudaError_t launch_observables(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s);
 cudaError_t launch_pairlist(const DevArrays& A, int r, int off, int n, cudaStream_t s);
+// packed (x y z per bead, replicas back to back at 3*poff[k]) <-> device state
+cudaError_t launch_scatter_state(const DevArrays& A, const int* ids, int nrep, const long long* poff,
+                                 const double* xyz, const double* vel, cudaStream_t s);
+cudaError_t launch_gather_state(const DevArrays& A, const int* ids, int nrep, const long long* poff,
+                                double* xyz, double* vel, cudaStream_t s);
 cudaError_t launch_export(const DevArrays& A, int r, int off, int n, int which, int cap,
                           cudaStream_t s);
 int step_kernel_max_smem();

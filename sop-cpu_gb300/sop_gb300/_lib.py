@@ -123,6 +123,8 @@ _PROTOS = {
     "sop_observables": (C.c_int, [VP, C.c_int, DP]),
     "sop_run_plain": (C.c_int, [VP, C.c_int, C.c_int64]),
     "sop_run": (C.c_int, [VP, C.c_int64]),
+    "sop_replica_start": (C.c_int, [VP, C.c_int, C.c_int64]),
+    "sop_run_chunk": (C.c_int, [VP, C.c_int64, IP, C.c_int, IP]),
     "sop_run_host": (C.c_int, [VP, DP, DP, C.c_int64, DP, DP]),
     "sop_last_run_timing": (C.c_int, [VP, DP, DP, C.POINTER(C.c_int64)]),
     "sop_profile_steps": (C.c_int, [VP, C.c_int64, DP, DP]),
