@@ -111,16 +111,18 @@ typedef struct sop_engine sop_engine;
 
 typedef struct sop_engine_config {
   int device;            /* CUDA ordinal                                       */
-  int max_beads;         /* bead capacity of the packed arrays (0 = 1<<20)     */
+  int max_beads;         /* bead capacity of the packed arrays (0 = 1<<21)     */
   int max_replicas;      /* replica slots (0 = 4096)                           */
   int64_t max_list_entries; /* neighbor-list entry capacity (0 = 64 per bead)  */
-  int block_threads;     /* fused step kernel block size (0 = 256)            */
-  int lanes_per_bead;    /* lanes cooperating on one bead: 1,2,4,8 (0 = 4)     */
+  int block_threads;     /* fused step kernel block size, 64..256 (0 = 256)   */
+  int lanes_per_bead;    /* lanes cooperating on one bead: 1,2,4,8,16 (0 = 2); the
+                            only knob that changes float summation order      */
   int graph_steps;       /* steps captured per CUDA graph launch (0 = 20)      */
   int stage_limit;       /* largest replica (beads) whose positions the step
                             kernel stages in shared memory by TMA; larger ones
-                            are gathered through L1 (0 = 6144, <0 = never)    */
-  int chunk_beads;       /* beads per step-kernel work item (0 = 256)          */
+                            are gathered through L1 (0 = 2048, <0 = never)    */
+  int chunk_beads;       /* beads per step-kernel work item (0 = 128)          */
+  int build_slice_beads; /* beads per list-build work unit, >= 16 (0 = 32)     */
 } sop_engine_config;
 
 /* ---- engine -------------------------------------------------------------- */
@@ -197,12 +199,28 @@ int sop_last_run_timing(sop_engine* e, double* total_ms, double* step_kernel_ms,
  * each kernel: mean device ms per launch of the fused step kernel and of the
  * prologue (bookkeeping + list builds + output-step energies). */
 int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_kernel_ms, double* prologue_ms);
+/* The same run split per kernel: ms[0..3] = mean k_decide, k_bin (cell
+ * binning), k_build (list slices, energies, observables), k_step per step. */
+int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms);
 
 /* ---- autotuner --------------------------------------------------------------- */
-/* Time the fused step for the active replicas over candidate block sizes,
- * lanes per bead, cell edges and skins; adopt the fastest per size bucket.
- * report (may be NULL) receives a text table of what was measured. */
+/* No reference counterpart.  Time the batched step of the active replicas
+ * over candidate launch shapes (step-kernel block size, beads per work item,
+ * shared-memory stage limit, beads per list-build slice; one choice for the
+ * engine) and, for replicas in
+ * skin mode, list skins and cell edges (one choice per size bucket
+ * [1,256) [256,1024) [1024,4096) [4096,...)); adopt the fastest.
+ * Every trial runs steps_per_trial warm-up plus steps_per_trial timed REAL
+ * steps inside one run window, so the call advances each active replica
+ * exactly as one sop_run of the reported step count would.  Launch-shape
+ * choices leave trajectories bit-identical; skin / cell-edge choices keep the
+ * pair sets exact but reorder list rows (float rounding only).  Call between
+ * runs.  report (may be NULL) receives a text table of the trials.
+ * sop_autotune tunes both groups. */
+#define SOP_TUNE_SHAPE 1
+#define SOP_TUNE_LISTS 2
 int sop_autotune(sop_engine* e, int steps_per_trial, char* report, int report_cap);
+int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, char* report, int report_cap);
 
 /* ---- continuous-batching server ----------------------------------------------- */
 typedef struct sop_server sop_server;

@@ -38,6 +38,9 @@ def _port_lib():
         L.sopo_set_topology_implicit.argtypes = [
             C.c_void_p, C.c_int, IP, IP, C.c_int, IP, IP, DP, C.c_int, IP, IP, IP,
             C.c_int, IP, IP, DP]
+        L.sopo_set_topology_pruned.argtypes = [
+            C.c_void_p, C.c_int, IP, IP, C.c_int, IP, IP, DP, C.c_int, IP, IP, IP,
+            C.c_int, IP, IP, DP, DP, C.c_double]
         L.sopo_set_coords.argtypes = [C.c_void_p, C.c_int, DP]
         L.sopo_get_coords.argtypes = [C.c_void_p, C.c_int, DP]
         L.sopo_set_param.argtypes = [C.c_void_p, C.c_char_p, C.c_double]
@@ -112,8 +115,10 @@ class Port:
             raise RuntimeError("sopo_load_script(%s) = %d" % (path, rc))
         return self.nbead
 
-    def set_system(self, system):
-        """Implicit-candidate topology from a sop_gb300.systems.System."""
+    def set_system(self, system, prune=None):
+        """Implicit-candidate topology from a sop_gb300.systems.System; with
+        `prune` (A), only the pairs closer than that at the system's positions
+        plus the natives (sopo_set_topology_pruned, for large systems)."""
         n = system.nbead
         ib, jb, r0 = [np.ascontiguousarray(a) for a in system.bonds]
         ia, ja, ka, _ = [np.ascontiguousarray(a) for a in system.angles]
@@ -126,13 +131,19 @@ class Port:
         ch = None if system.chain is None else np.ascontiguousarray(system.chain, np.int32)
         ip = lambda a: a.ctypes.data_as(IP) if a is not None else None
         dp = lambda a: a.ctypes.data_as(DP)
-        self._keep = (ib, jb, r0, ia, ja, ka, in_, jn, rn, typ, ch)
-        rc = self.L.sopo_set_topology_implicit(self.h, n, ip(typ), ip(ch), len(ib), ip(ib), ip(jb),
-                                               dp(r0), len(ia), ip(ia), ip(ja), ip(ka), len(in_),
-                                               ip(in_), ip(jn), dp(rn))
-        if rc != 0:
-            raise RuntimeError("sopo_set_topology_implicit = %d" % rc)
         xyz = np.ascontiguousarray(system.xyz, np.float64)
+        self._keep = (ib, jb, r0, ia, ja, ka, in_, jn, rn, typ, ch, xyz)
+        if prune is None:
+            rc = self.L.sopo_set_topology_implicit(self.h, n, ip(typ), ip(ch), len(ib), ip(ib),
+                                                   ip(jb), dp(r0), len(ia), ip(ia), ip(ja), ip(ka),
+                                                   len(in_), ip(in_), ip(jn), dp(rn))
+        else:
+            rc = self.L.sopo_set_topology_pruned(self.h, n, ip(typ), ip(ch), len(ib), ip(ib),
+                                                 ip(jb), dp(r0), len(ia), ip(ia), ip(ja), ip(ka),
+                                                 len(in_), ip(in_), ip(jn), dp(rn), dp(xyz),
+                                                 float(prune))
+        if rc != 0:
+            raise RuntimeError("sopo_set_topology = %d" % rc)
         self.set_coords(0, xyz)
         self.set_coords(1, xyz)
 

@@ -293,6 +293,128 @@ int sopo_set_topology_implicit(sopo_sys* s, int nbead, const int* type, const in
   return 0;
 }
 
+static int cmp_ll(const void* a, const void* b) {
+  const long long x = *(const long long*)a, y = *(const long long*)b;
+  return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+int sopo_set_topology_pruned(sopo_sys* s, int nbead, const int* type, const int* chain,
+                             int nbnd, const int* ib, const int* jb, const double* r0,
+                             int nang, const int* ia, const int* ja, const int* ka,
+                             int nnat, const int* in_, const int* jn, const double* rn,
+                             const double* xyz, double cutoff) {
+  if (nbead <= 0 || !(cutoff > 0)) return -1;
+  /* close pairs (i<j) through a uniform grid of edge `cutoff` */
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int i = 0; i < nbead; i++)
+    for (int c = 0; c < 3; c++) {
+      if (xyz[3 * i + c] < lo[c]) lo[c] = xyz[3 * i + c];
+      if (xyz[3 * i + c] > hi[c]) hi[c] = xyz[3 * i + c];
+    }
+  long long dim[3];
+  double edge = cutoff;
+  for (;;) {
+    for (int c = 0; c < 3; c++) dim[c] = (long long)((hi[c] - lo[c]) / edge) + 1;
+    if (dim[0] * dim[1] * dim[2] <= 4LL * nbead + 4096) break;
+    edge *= 1.25;
+  }
+  const long long ncell = dim[0] * dim[1] * dim[2];
+  long long* cid = (long long*)xcalloc((size_t)nbead, sizeof(long long));
+  long long* start = (long long*)xcalloc((size_t)ncell + 1, sizeof(long long));
+  int* sorted = (int*)xcalloc((size_t)nbead, sizeof(int));
+  for (int i = 0; i < nbead; i++) {
+    long long q[3];
+    for (int c = 0; c < 3; c++) {
+      q[c] = (long long)((xyz[3 * i + c] - lo[c]) / edge);
+      if (q[c] >= dim[c]) q[c] = dim[c] - 1;
+    }
+    cid[i] = q[0] + dim[0] * (q[1] + dim[1] * q[2]);
+    start[cid[i] + 1]++;
+  }
+  for (long long c = 0; c < ncell; c++) start[c + 1] += start[c];
+  {
+    long long* fill = (long long*)xcalloc((size_t)ncell, sizeof(long long));
+    for (int i = 0; i < nbead; i++) sorted[start[cid[i]] + fill[cid[i]]++] = i;
+    free(fill);
+  }
+  size_t cap = 1024, np = 0;
+  long long* pairs = (long long*)xcalloc(cap, sizeof(long long));
+  const double c2 = cutoff * cutoff;
+  for (int i = 0; i < nbead; i++) {
+    const long long qx = cid[i] % dim[0], qy = (cid[i] / dim[0]) % dim[1], qz = cid[i] / (dim[0] * dim[1]);
+    for (long long z = qz - 1; z <= qz + 1; z++)
+      for (long long y = qy - 1; y <= qy + 1; y++)
+        for (long long x = qx - 1; x <= qx + 1; x++) {
+          if (x < 0 || y < 0 || z < 0 || x >= dim[0] || y >= dim[1] || z >= dim[2]) continue;
+          const long long cc = x + dim[0] * (y + dim[1] * z);
+          for (long long k = start[cc]; k < start[cc + 1]; k++) {
+            const int j = sorted[k];
+            if (j <= i) continue;
+            if (!((chain && chain[i] != chain[j]) || j - i > 2)) continue;
+            const double dx = xyz[3 * j] - xyz[3 * i], dy = xyz[3 * j + 1] - xyz[3 * i + 1],
+                         dz = xyz[3 * j + 2] - xyz[3 * i + 2];
+            if (dx * dx + dy * dy + dz * dz >= c2) continue;
+            if (np == cap) {
+              cap *= 2;
+              pairs = (long long*)realloc(pairs, cap * sizeof(long long));
+              if (!pairs) { fprintf(stderr, "oracle: out of memory\n"); exit(1); }
+            }
+            pairs[np++] = (long long)i * nbead + j;
+          }
+        }
+  }
+  free(cid);
+  free(start);
+  free(sorted);
+  /* every native pair (i<j) is a candidate whatever its distance */
+  for (int k = 0; k < nnat; k++) {
+    if (np == cap) {
+      cap *= 2;
+      pairs = (long long*)realloc(pairs, cap * sizeof(long long));
+      if (!pairs) { fprintf(stderr, "oracle: out of memory\n"); exit(1); }
+    }
+    pairs[np++] = (long long)in_[k] * nbead + jn[k];
+  }
+  qsort(pairs, np, sizeof(long long), cmp_ll);
+  size_t u = 0;
+  for (size_t k = 0; k < np; k++)
+    if (u == 0 || pairs[k] != pairs[u - 1]) pairs[u++] = pairs[k];
+  np = u;
+
+  alloc_beads(s, nbead);
+  set_bonds(s, nbnd, ib, jb, r0);
+  set_angles(s, nang, ia, ja, ka);
+  int* nat = (int*)xcalloc(3 * (size_t)(nnat > 0 ? nnat : 1), sizeof(int));
+  for (int k = 0; k < nnat; k++) { nat[3 * k] = in_[k]; nat[3 * k + 1] = jn[k]; nat[3 * k + 2] = k; }
+  qsort(nat, nnat, 3 * sizeof(int), cmp_pair);
+  int nnative = 0;
+  for (int k = 0; k < nnat; k++) {
+    int t_i = type ? type[in_[k]] : 1, t_j = type ? type[jn[k]] : 1;
+    if (rn[k] < k_rcut_nat[t_i][t_j]) nnative++;
+  }
+  alloc_candidates(s, nnative, (int)(np - (size_t)nnative));
+  int nn = 0, nr = 0, p = 0;
+  for (size_t k = 0; k < np; k++) {
+    const int i = (int)(pairs[k] / nbead), j = (int)(pairs[k] % nbead);
+    if (!((chain && chain[i] != chain[j]) || j - i > 2)) continue;  /* not a candidate */
+    int ti = type ? type[i] : 1, tj = type ? type[j] : 1;
+    while (p < nnat && (nat[3 * p] < i || (nat[3 * p] == i && nat[3 * p + 1] < j))) p++;
+    if (p < nnat && nat[3 * p] == i && nat[3 * p + 1] == j &&
+        rn[nat[3 * p + 2]] < k_rcut_nat[ti][tj]) {
+      put_native(s, nn++, i, j, rn[nat[3 * p + 2]], ti, tj);
+    } else {
+      s->ri[nr] = i; s->rj[nr] = j; s->rti[nr] = ti; s->rtj[nr] = tj;
+      nr++;
+    }
+  }
+  free(nat);
+  free(pairs);
+  s->nnat = nn;
+  s->nrep = nr;
+  seed_pair_lists(s);
+  return 0;
+}
+
 static double* coord_ptr(const sopo_sys* s, int which) {
   switch (which) {
     case 0: return s->pos;

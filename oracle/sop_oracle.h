@@ -48,6 +48,18 @@ int sopo_set_topology_implicit(sopo_sys* s, int nbead, const int* type, const in
                                int nbnd, const int* ib, const int* jb, const double* r0,
                                int nang, const int* ia, const int* ja, const int* ka,
                                int nnat, const int* in_, const int* jn, const double* rn);
+/* The implicit candidate set restricted, for large systems, to the pairs
+ * closer than `cutoff` at positions xyz (found through a cell grid), plus
+ * every native pair; lexicographic order as above, so every list and sum the
+ * reference forms over the full set is formed over this one in the same order
+ * as long as no pair beyond `cutoff` could enter a list (the caller picks the
+ * cutoff above the list cutoffs plus the motion it runs).  The
+ * reference's own large-N recipe: pair lists filled from a CPU cell list. */
+int sopo_set_topology_pruned(sopo_sys* s, int nbead, const int* type, const int* chain,
+                             int nbnd, const int* ib, const int* jb, const double* r0,
+                             int nang, const int* ia, const int* ja, const int* ka,
+                             int nnat, const int* in_, const int* jn, const double* rn,
+                             const double* xyz, double cutoff);
 
 /* which: 0 pos, 1 unc_pos, 2 vel, 3 force, 4 incr (3*nbead doubles) */
 int sopo_set_coords(sopo_sys* s, int which, const double* xyz);

@@ -190,6 +190,7 @@ extern "C" void sop_engine_config_default(sop_engine_config* c) {
   c->graph_steps = 20;
   c->stage_limit = 2048;
   c->chunk_beads = 128;
+  c->build_slice_beads = kSliceBeads;
 }
 
 // ---- engine lifetime ------------------------------------------------------------
@@ -214,9 +215,11 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
     if (cfg_in->graph_steps > 0) cfg.graph_steps = cfg_in->graph_steps;
     if (cfg_in->stage_limit != 0) cfg.stage_limit = cfg_in->stage_limit;
     if (cfg_in->chunk_beads > 0) cfg.chunk_beads = cfg_in->chunk_beads;
+    if (cfg_in->build_slice_beads > 0) cfg.build_slice_beads = cfg_in->build_slice_beads;
   }
   if (cfg.stage_limit > kStageMax) cfg.stage_limit = kStageMax;
   if (cfg.chunk_beads < 32) cfg.chunk_beads = 32;
+  if (cfg.build_slice_beads < kMinSliceBeads) cfg.build_slice_beads = kMinSliceBeads;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
     cudaGetLastError();
@@ -264,7 +267,10 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(dalloc(&A.err, 1));
   CK(cudaMemsetAsync(A.err, 0, sizeof(int), e->stream));
   // unit queue: every replica may queue all its build slices plus two units
-  A.unit_cap = cfg.max_replicas * (kBuildMax / kSliceBeads + 2);
+  A.slice_beads = cfg.build_slice_beads;
+  // every replica may queue all its build slices (at the smallest slice size)
+  // plus an energy and an observables unit
+  A.unit_cap = (int)std::min<long long>(cap / kMinSliceBeads + 3LL * cfg.max_replicas + 64, 1LL << 30);
   CK(dalloc(&A.units, A.unit_cap));
   CK(dalloc(&A.unit_cnt, 2));
   A.unit_exit = A.unit_cnt + 1;
@@ -276,6 +282,20 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(cudaMemsetAsync(A.done_cnt, 0, sizeof(int), e->stream));
   CK(cudaMemsetAsync(A.slice_done, 0, sizeof(int) * cfg.max_replicas, e->stream));
   CK(cudaMemsetAsync(A.rep, 0, sizeof(RepDev) * cfg.max_replicas, e->stream));
+  // cell bins of the list builds: per bead, and a cell range per replica
+  const long long cellcap = 4 * cap + 4104LL * cfg.max_replicas;
+  CK(dalloc(&A.bin_p, cap));
+  CK(dalloc(&A.bin_sorted, cap));
+  CK(dalloc(&A.bin_cell, cap));
+  CK(dalloc(&A.cstart, cellcap));
+  CK(dalloc(&A.ccur, cellcap));
+  CK(dalloc(&A.bin_hdr, cfg.max_replicas));
+  A.bin_cap = cfg.max_replicas;
+  CK(dalloc(&A.bins, A.bin_cap));
+  CK(dalloc(&A.bin_cnt, 2));
+  A.bin_exit = A.bin_cnt + 1;
+  CK(cudaMemsetAsync(A.bin_cnt, 0, 2 * sizeof(int), e->stream));
+  e->cells.init(cellcap);
   CK(dalloc(&e->d_ids, cfg.max_replicas + 4));
   CK(dalloc(&e->d_items, cap / 32 + cfg.max_replicas + 16));
   e->items_cap = cap / 32 + cfg.max_replicas + 16;
@@ -318,7 +338,8 @@ extern "C" int sop_engine_destroy(sop_engine* e) {
                   A.exc_rng, A.nl_cnt, A.nl, A.nat, A.nat_r0, A.bnd, A.bnd_r0, A.ang, A.exc,
                   A.rep, A.pairs_out, A.pairs_cnt, A.err, A.units, A.unit_cnt, A.slice_done,
                   A.done_list, A.done_cnt, e->d_ids, e->d_items, e->d_counts, e->d_pack_xyz,
-                  e->d_pack_vel, e->d_pack_ids, e->d_pack_off};
+                  e->d_pack_vel, e->d_pack_ids, e->d_pack_off, A.bin_p, A.bin_sorted,
+                  A.bin_cell, A.cstart, A.ccur, A.bin_hdr, A.bins, A.bin_cnt};
   for (void* p : ptrs) cudaFree(p);
   if (e->h_rep) cudaFreeHost(e->h_rep);
   for (int k = 0; k < 4; k++) if (e->ev[k]) cudaEventDestroy(e->ev[k]);
@@ -570,6 +591,7 @@ extern "C" int sop_system_bytes(const sop_engine* e, const sop_system_desc* d, i
   long long L = compute_L(d, T, d->params.list_mode);
   long long n = d->nbead;
   long long b = n * (2 * 24 + 2 * 32 + 12 + 24 + 24 + 16 + 16 + 8 + 4) + n * L * 4 +
+                n * (16 + 4 + 4) + (cell_capacity((int)n) + 1) * 8 +
                 (long long)T.nat.size() * 16 + (long long)T.bnd.size() * 24 +
                 (long long)T.ang.size() * 4 + (long long)T.exc.size() * 4;
   *bytes = b;
@@ -651,14 +673,13 @@ static bool live(const sop_engine* e, int r) {
 // Build the lists of replica r from its current positions (single CTA).
 int sop::build_now(sop_engine* e, int r, int mode) {
   Replica& R = e->reps[r];
-  if (R.n > kBuildMax) return SOP_ERR_UNSUPPORTED;
   int id = r;
   CK(cudaMemcpyAsync(e->d_ids + scratch_id(e, 0), &id, sizeof(int), cudaMemcpyHostToDevice,
                      e->stream));
-  const int nsl = (R.n + kSliceBeads - 1) / kSliceBeads;
-  CK(launch_prologue(e->A, e->d_ids + scratch_id(e, 0), 1, nullptr, R.n, 1, mode,
+  const int nsl = (R.n + e->A.slice_beads - 1) / e->A.slice_beads;
+  CK(launch_prologue(e->A, e->d_ids + scratch_id(e, 0), 1, nullptr, 1, mode,
                      std::min(nsl, 2 * e->prop.multiProcessorCount), e->stream));
-  e->launches += 2;
+  e->launches += kPrologueLaunches;
   CK(cudaStreamSynchronize(e->stream));
   return SOP_OK;
 }
@@ -668,7 +689,7 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
   if ((d->nbnd && (!d->ib || !d->jb || !d->r0)) || (d->nang && (!d->ia || !d->ka)) ||
       (d->nnat && (!d->in_ || !d->jn || !d->rn)) || (d->nexcl && (!d->ie || !d->je)))
     return SOP_ERR_ARG;
-  if (d->nbead > kBuildMax) return SOP_ERR_UNSUPPORTED;
+  if (d->nbead > kMaxReplicaBeads) return SOP_ERR_UNSUPPORTED;
   for (long long q = 0; q < 3LL * d->nbead; q++)
     if (!std::isfinite(d->xyz[q])) return SOP_ERR_ARG;
   RepDev rd;
@@ -684,20 +705,32 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
   if (slot < 0) return SOP_ERR_FULL;
   const int n = d->nbead;
   const int L = compute_L(d, T, d->params.list_mode);
-  long long off, nlb, nb, bb, ab, xb;
-  if (!e->beads.alloc(n, 8, &off)) return SOP_ERR_FULL;
-  if (!e->lists.alloc((long long)n * L, 8, &nlb)) { e->beads.release(off, n); return SOP_ERR_FULL; }
-  if (!e->nats.alloc((long long)T.nat.size(), 1, &nb) || !e->bnds.alloc((long long)T.bnd.size(), 1, &bb) ||
-      !e->angs.alloc((long long)T.ang.size(), 1, &ab) || !e->excs.alloc((long long)T.exc.size(), 1, &xb)) {
-    // partial allocations are returned below via a temporary replica record
-    e->beads.release(off, n);
-    e->lists.release(nlb, (long long)n * L);
-    return SOP_ERR_FULL;
+  const long long ncell_e = cell_capacity(n) + 1;
+  long long off = 0, nlb = 0, nb = 0, bb = 0, ab = 0, xb = 0, cb = 0;
+  {
+    // all ranges or none
+    struct Want { RangeAlloc* a; long long n, align; long long* out; };
+    const Want want[] = {{&e->beads, n, 8, &off},
+                         {&e->lists, (long long)n * L, 8, &nlb},
+                         {&e->nats, (long long)T.nat.size(), 1, &nb},
+                         {&e->bnds, (long long)T.bnd.size(), 1, &bb},
+                         {&e->angs, (long long)T.ang.size(), 1, &ab},
+                         {&e->excs, (long long)T.exc.size(), 1, &xb},
+                         {&e->cells, ncell_e, 8, &cb}};
+    const int nw = (int)(sizeof want / sizeof want[0]);
+    for (int k = 0; k < nw; k++) {
+      if (!want[k].a->alloc(want[k].n, want[k].align, want[k].out)) {
+        for (int q = 0; q < k; q++) want[q].a->release(*want[q].out, want[q].n);
+        return SOP_ERR_FULL;
+      }
+    }
   }
   Replica& R = e->reps[slot];
   R = Replica();
   R.live = true;
   R.n = n;
+  R.cell_base = cb;
+  R.ncell_e = ncell_e;
   R.off = off;
   R.nl_base = nlb;
   R.L = L;
@@ -733,6 +766,8 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
   rd.nl_base = nlb;
   rd.L = L;
   rd.nat_base = (int)nb; rd.bnd_base = (int)bb; rd.ang_base = (int)ab; rd.exc_base = (int)xb;
+  rd.cell_base = cb;
+  rd.cell_cap = (int)cell_capacity(n);
   int pi = d->params.pull_i, pj = d->params.pull_j;
   rd.pull_i = (pi >= 0 && pi < n) ? pi : 0;
   rd.pull_j = (pj >= 0 && pj < n) ? pj : n - 1;
@@ -747,35 +782,54 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
   rc = upload_velocities(e, slot, d->vel);
   if (rc) return rc;
   // set-up of underdamped_ctrl (sop.cpp:117-125): lists at the initial positions
-  rc = build_now(e, slot, d->params.list_mode);
-  if (rc) return rc;
-  // rows sized from a host estimate; if the build found a longer row, grow
-  // the replica's list range to fit it with room to spare and build again
-  for (int attempt = 0; attempt < 3; attempt++) {
-    RepDev got;
-    rc = get_rep(e, slot, &got);
-    if (rc) return rc;
-    if (!(got.status & SOP_ST_LIST_OVERFLOW)) break;
-    const int L2 = ((got.max_row + got.max_row / 2 + 32) + 7) / 8 * 8;
-    long long nlb2;
-    e->lists.release(R.nl_base, (long long)n * R.L);
-    if (!e->lists.alloc((long long)n * L2, 8, &nlb2)) {
-      sop_replica_remove(e, slot);
-      return SOP_ERR_FULL;
-    }
-    R.nl_base = nlb2;
-    R.L = L2;
-    got.nl_base = nlb2;
-    got.L = L2;
-    got.status &= ~SOP_ST_LIST_OVERFLOW;
-    rc = put_rep(e, slot, got);
-    if (rc) return rc;
-    rc = build_now(e, slot, d->params.list_mode);
-    if (rc) return rc;
+  rc = rebuild_fit(e, slot, d->params.list_mode);
+  if (rc) {
+    if (rc == SOP_ERR_FULL) sop_replica_remove(e, slot);
+    return rc;
   }
   e->layout_dirty = true;
   *replica = slot;
   return SOP_OK;
+}
+
+// Move replica r's list rows to a range of row length >= need (+50% and 32
+// spare), releasing the old range; the caller rebuilds.  Clears the overflow
+// status.  SOP_ERR_FULL (old range kept) when the list arena has no room.
+int sop::grow_rows(sop_engine* e, int r, int need) {
+  Replica& R = e->reps[r];
+  const int L2 = ((need + need / 2 + 32) + 7) / 8 * 8;
+  long long nlb2;
+  if (!e->lists.alloc((long long)R.n * L2, 8, &nlb2)) return SOP_ERR_FULL;
+  RepDev got;
+  int rc = get_rep(e, r, &got);
+  if (rc) return rc;
+  e->lists.release(R.nl_base, (long long)R.n * R.L);
+  R.nl_base = nlb2;
+  R.L = L2;
+  got.nl_base = nlb2;
+  got.L = L2;
+  got.status &= ~SOP_ST_LIST_OVERFLOW;
+  return put_rep(e, r, got);
+}
+
+// Build replica r's lists now; rows sized from a host estimate grow (up to
+// three times) when the build finds a longer row.
+int sop::rebuild_fit(sop_engine* e, int r, int mode) {
+  int rc = build_now(e, r, mode);
+  for (int attempt = 0; rc == SOP_OK && attempt < 3; attempt++) {
+    RepDev got;
+    rc = get_rep(e, r, &got);
+    if (rc) return rc;
+    if (!(got.status & SOP_ST_LIST_OVERFLOW)) return SOP_OK;
+    rc = grow_rows(e, r, got.max_row);
+    if (rc) return rc;
+    rc = build_now(e, r, mode);
+  }
+  if (rc) return rc;
+  RepDev got;
+  rc = get_rep(e, r, &got);
+  if (rc) return rc;
+  return (got.status & SOP_ST_LIST_OVERFLOW) ? SOP_ERR_OVERFLOW : SOP_OK;
 }
 
 extern "C" int sop_replica_remove(sop_engine* e, int r) {
@@ -792,6 +846,7 @@ extern "C" int sop_replica_remove(sop_engine* e, int r) {
   e->bnds.release(R.bnd_base, R.nbnd_e);
   e->angs.release(R.ang_base, R.nang_e);
   e->excs.release(R.exc_base, R.nexc_e);
+  e->cells.release(R.cell_base, R.ncell_e);
   R = Replica();
   e->layout_dirty = true;
   return SOP_OK;
@@ -832,9 +887,9 @@ extern "C" int sop_replica_set_params(sop_engine* e, int r, const sop_params* p)
   rc = put_rep(e, r, d);
   if (rc) return rc;
   if (mode_changed) {
-    // a new list mode may need longer rows than the replica holds
+    // a new list mode or skin may need longer rows than the replica holds
     if (p->list_mode == SOP_LIST_NONE && R.L < R.n) return SOP_ERR_UNSUPPORTED;
-    rc = build_now(e, r, p->list_mode);
+    rc = rebuild_fit(e, r, p->list_mode);
   }
   e->graph_valid = false;
   return rc;
@@ -897,7 +952,7 @@ extern "C" int sop_replica_set_state(sop_engine* e, int r, const double* unc_pos
   if (rc) return rc;
   // lists for the new positions (the reference builds them before loading a
   // restart, sop.cpp:119-136, and runs on stale lists until the next rebuild)
-  return build_now(e, r, e->reps[r].params.list_mode);
+  return rebuild_fit(e, r, e->reps[r].params.list_mode);
 }
 
 extern "C" int sop_replica_status(sop_engine* e, int r, int* status, int64_t* steps) {
@@ -958,41 +1013,33 @@ int sop::refresh_layout(sop_engine* e) {
     e->items.insert(e->items.end(), it.begin(), it.end());
   }
   if ((long long)e->items.size() + 64 > e->items_cap) return SOP_ERR_FULL;
-  // the kernels read the counts from device memory, so a captured graph stays
-  // valid; only a new shared-memory size class for k_build needs a recapture
+  // the kernels read the counts from device memory, so a captured graph stays valid
   const int counts[2] = {(int)ids.size(), (int)e->items.size()};
   if (!ids.empty()) CK(h2d(e->d_ids, ids.data(), ids.size(), e->stream));
   if (!e->items.empty()) CK(h2d(e->d_items, e->items.data(), e->items.size(), e->stream));
   CK(h2d(e->d_counts, counts, 2, e->stream));
-  int bucket = 1024;
-  while (bucket < e->max_n) bucket <<= 1;
-  bucket = std::min(bucket, kBuildMax);
-  if (bucket != e->build_bucket) {
-    e->build_bucket = bucket;
-    e->graph_valid = false;
-  }
   e->layout_dirty = false;
   return SOP_OK;
 }
 
 // One step over given ids / items with host counts (single-replica paths).
 int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items,
-                      int nitems, int max_n, int max_staged, int step_grid, int pro_grid) {
-  CK(launch_prologue(e->A, d_ids, nrep, nullptr, max_n, 0, 0, pro_grid, e->stream));
+                      int nitems, int max_staged, int step_grid, int pro_grid) {
+  CK(launch_prologue(e->A, d_ids, nrep, nullptr, 0, 0, pro_grid, e->stream));
   CK(launch_step(e->A, d_items, nitems, nullptr, max_staged, e->cfg.lanes_per_bead,
                  e->cfg.block_threads, step_grid, e->stream));
-  e->launches += 3;
+  e->launches += kStepLaunches;
   return SOP_OK;
 }
 
-// One batched step: k_decide, k_build (builds, energies, observables), k_step,
-// sized by the engine's fixed grids and the device-resident counts.
+// One batched step: k_decide, k_bin + k_build (builds, energies, observables),
+// k_step, sized by the engine's fixed grids and the device-resident counts.
 int sop::enqueue_batched_step(sop_engine* e) {
-  CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, e->build_bucket, 0, 0,
+  CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0,
                      e->pro_grid, e->stream));
   CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, e->max_staged,
                  e->cfg.lanes_per_bead, e->cfg.block_threads, e->step_grid, e->stream));
-  e->launches += 3;
+  e->launches += kStepLaunches;
   return SOP_OK;
 }
 
@@ -1040,14 +1087,14 @@ extern "C" int sop_run_plain(sop_engine* e, int r, int64_t nsteps) {
   CK(cudaGetLastError());
   CK(cudaEventRecord(e->ev[0], e->stream));
   const int grid = std::min((int)items.size(), 4 * e->prop.multiProcessorCount);
-  const int bgrid = std::min((R.n + kSliceBeads - 1) / kSliceBeads + 1, 2 * e->prop.multiProcessorCount);
+  const int bgrid = std::min((R.n + e->A.slice_beads - 1) / e->A.slice_beads + 1,
+                             2 * e->prop.multiProcessorCount);
   for (int64_t s = 0; s <= nsteps; s++) {
-    int rc = enqueue_step(e, e->d_ids + id_slot, 1, e->d_items + item_slot, (int)items.size(), R.n,
+    int rc = enqueue_step(e, e->d_ids + id_slot, 1, e->d_items + item_slot, (int)items.size(),
                           staged ? R.n : 0, grid, bgrid);
     if (rc) return rc;
   }
-  CK(launch_observables(e->A, e->d_ids + id_slot, 1, e->stream));
-  e->launches++;
+  // observables are computed on demand (sop_observables), not at run end
   CK(cudaEventRecord(e->ev[1], e->stream));
   CK(cudaStreamSynchronize(e->stream));
   float ms = 0;
@@ -1094,14 +1141,13 @@ int sop::run_batched(sop_engine* e, int64_t nsteps, bool timed) {
   const int64_t full = iters / S;
   for (int64_t k = 0; k < full; k++) {
     CK(cudaGraphLaunch(e->graph_exec, e->stream));
-    e->launches += 3 * S;
+    e->launches += kStepLaunches * S;
   }
   for (int64_t k = full * S; k < iters; k++) {
     rc = enqueue_batched_step(e);
     if (rc) return rc;
   }
-  CK(launch_observables(e->A, e->d_ids, nrep, e->stream));
-  e->launches++;
+  // observables are computed on demand (sop_observables), not at run end
   if (timed) CK(cudaEventRecord(e->ev[1], e->stream));
   CK(cudaStreamSynchronize(e->stream));
   if (timed) {
@@ -1139,7 +1185,7 @@ extern "C" int sop_run_chunk(sop_engine* e, int64_t steps, int* finished, int ca
   const int S = e->cfg.graph_steps;
   for (int64_t k = 0; k < steps / S; k++) {
     CK(cudaGraphLaunch(e->graph_exec, e->stream));
-    e->launches += 3 * S;
+    e->launches += kStepLaunches * S;
   }
   for (int64_t k = steps / S * S; k < steps; k++) {
     rc = enqueue_batched_step(e);
@@ -1159,6 +1205,54 @@ extern "C" int sop_run_chunk(sop_engine* e, int64_t steps, int* finished, int ca
   return check_errors(e);
 }
 
+int sop::begin_all(sop_engine* e, int64_t nsteps) {
+  int rc = refresh_layout(e);
+  if (rc) return rc;
+  const int nrep = (int)e->active.size();
+  if (nrep == 0) return SOP_ERR_STATE;
+  k_begin<<<(nrep + 127) / 128, 128, 0, e->stream>>>(e->A.rep, e->d_ids, nrep, nsteps);
+  e->launches++;
+  CK(cudaGetLastError());
+  return SOP_OK;
+}
+
+int sop::run_steps(sop_engine* e, int64_t steps, float* ms) {
+  int rc = refresh_layout(e);
+  if (rc) return rc;
+  rc = capture_graph(e);
+  if (rc) return rc;
+  CK(cudaEventRecord(e->ev[0], e->stream));
+  const int S = e->cfg.graph_steps;
+  for (int64_t k = 0; k < steps / S; k++) {
+    CK(cudaGraphLaunch(e->graph_exec, e->stream));
+    e->launches += kStepLaunches * S;
+  }
+  for (int64_t k = steps / S * S; k < steps; k++) {
+    rc = enqueue_batched_step(e);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(e->ev[1], e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  float t = 0;
+  cudaEventElapsedTime(&t, e->ev[0], e->ev[1]);
+  if (ms) *ms = t;
+  return check_errors(e);
+}
+
+void sop::set_launch_shape(sop_engine* e, int threads, int chunk_beads, int stage_limit,
+                           int slice_beads) {
+  e->cfg.block_threads = threads;
+  e->cfg.build_slice_beads = std::max(slice_beads, kMinSliceBeads);
+  e->A.slice_beads = e->cfg.build_slice_beads;
+  e->cfg.chunk_beads = chunk_beads;
+  e->cfg.stage_limit = std::min(stage_limit, kStageMax);
+  e->max_staged = e->cfg.stage_limit > 0 ? e->cfg.stage_limit : 0;
+  e->step_grid = std::max(1, step_blocks_per_sm(e->cfg.lanes_per_bead, threads, e->max_staged)) *
+                 e->prop.multiProcessorCount;
+  e->layout_dirty = true;
+  e->graph_valid = false;
+}
+
 extern "C" int sop_run(sop_engine* e, int64_t nsteps) {
   if (!e || nsteps < 0) return SOP_ERR_ARG;
   CK(cudaSetDevice(e->cfg.device));
@@ -1174,8 +1268,8 @@ extern "C" int sop_last_run_timing(sop_engine* e, double* total_ms, double* step
   return SOP_OK;
 }
 
-extern "C" int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_ms, double* pro_ms) {
-  if (!e || nsteps <= 0) return SOP_ERR_ARG;
+extern "C" int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms) {
+  if (!e || nsteps <= 0 || !ms) return SOP_ERR_ARG;
   CK(cudaSetDevice(e->cfg.device));
   int rc = refresh_layout(e);
   if (rc) return rc;
@@ -1184,31 +1278,40 @@ extern "C" int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_ms,
   k_begin<<<(nrep + 127) / 128, 128, 0, e->stream>>>(e->A.rep, e->d_ids, nrep, nsteps);
   e->launches++;
   const int64_t iters = nsteps + 1;
-  std::vector<cudaEvent_t> ev(3 * iters);
+  constexpr int kE = 5;  // before k_decide, after k_decide, after k_bin, after k_build, after k_step
+  std::vector<cudaEvent_t> ev(kE * iters);
   for (auto& x : ev) CK(cudaEventCreate(&x));
   for (int64_t s = 0; s < iters; s++) {
-    CK(cudaEventRecord(ev[3 * s], e->stream));
-    CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, e->build_bucket, 0, 0,
-                       e->pro_grid, e->stream));
-    CK(cudaEventRecord(ev[3 * s + 1], e->stream));
+    cudaEvent_t* E = &ev[kE * s];
+    CK(cudaEventRecord(E[0], e->stream));
+    CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0, e->pro_grid,
+                       e->stream, E[1], E[2]));
+    CK(cudaEventRecord(E[3], e->stream));
     CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, e->max_staged,
                    e->cfg.lanes_per_bead, e->cfg.block_threads, e->step_grid, e->stream));
-    CK(cudaEventRecord(ev[3 * s + 2], e->stream));
-    e->launches += 3;
+    CK(cudaEventRecord(E[4], e->stream));
+    e->launches += kStepLaunches;
   }
   CK(cudaStreamSynchronize(e->stream));
-  double ts = 0, tp = 0;
-  for (int64_t s = 0; s < iters; s++) {
-    float a = 0, b = 0;
-    cudaEventElapsedTime(&a, ev[3 * s], ev[3 * s + 1]);
-    cudaEventElapsedTime(&b, ev[3 * s + 1], ev[3 * s + 2]);
-    tp += a;
-    ts += b;
-  }
+  double acc[4] = {0, 0, 0, 0};
+  for (int64_t s = 0; s < iters; s++)
+    for (int k = 0; k < 4; k++) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[kE * s + k], ev[kE * s + k + 1]);
+      acc[k] += t;
+    }
   for (auto& x : ev) cudaEventDestroy(x);
-  if (step_ms) *step_ms = ts / iters;
-  if (pro_ms) *pro_ms = tp / iters;
+  for (int k = 0; k < 4; k++) ms[k] = acc[k] / iters;
   return check_errors(e);
+}
+
+extern "C" int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_ms, double* pro_ms) {
+  double ms[4];
+  int rc = sop_profile_steps_ex(e, nsteps, ms);
+  if (rc) return rc;
+  if (step_ms) *step_ms = ms[3];
+  if (pro_ms) *pro_ms = ms[0] + ms[1] + ms[2];
+  return SOP_OK;
 }
 
 extern "C" int sop_run_host(sop_engine* e, const double* xyz_in, const double* vel_in,
@@ -1234,8 +1337,8 @@ extern "C" int sop_run_host(sop_engine* e, const double* xyz_in, const double* v
   if (vel_in) CK(h2d(e->d_pack_vel, vel_in, 3 * total, e->stream));
   CK(launch_scatter_state(e->A, e->d_pack_ids, nrep, e->d_pack_off, e->d_pack_xyz,
                           vel_in ? e->d_pack_vel : nullptr, e->stream));
-  CK(launch_prologue(e->A, e->d_pack_ids, nrep, nullptr, e->max_n, 1, -1, e->pro_grid, e->stream));
-  e->launches += 3;
+  CK(launch_prologue(e->A, e->d_pack_ids, nrep, nullptr, 1, -1, e->pro_grid, e->stream));
+  e->launches += kPrologueLaunches;
   rc = run_batched(e, nsteps, false);
   if (rc) return rc;
   // gather on the device, one copy out

@@ -40,7 +40,7 @@ struct Replica {
   long long off = 0, nl_base = 0;
   int L = 0;
   long long nat_base = 0, nnat_e = 0, bnd_base = 0, nbnd_e = 0, ang_base = 0, nang_e = 0,
-            exc_base = 0, nexc_e = 0;
+            exc_base = 0, nexc_e = 0, cell_base = 0, ncell_e = 0;
   int nnat_pairs = 0;
   sop_params params{};
   std::vector<int> type, chain;
@@ -56,7 +56,7 @@ struct sop_engine {
   cudaStream_t stream = nullptr;
   sop::DevArrays A{};
   long long cap = 0;
-  sop::RangeAlloc beads, lists, nats, bnds, angs, excs;
+  sop::RangeAlloc beads, lists, nats, bnds, angs, excs, cells;
   std::vector<sop::Replica> reps;
   sop::RepDev* h_rep = nullptr;  // pinned staging for descriptor copies
   // batched layout
@@ -67,7 +67,6 @@ struct sop_engine {
   std::vector<sop::StepItem> items;
   int max_n = 0, max_staged = 0, step_grid = 1, pro_grid = 1;
   int* d_counts = nullptr;          // {active replicas, work items}, read by the kernels
-  int build_bucket = 0;             // k_build shared-memory size class (beads)
   // packed host-order state of sop_run_host (one copy each way)
   double* d_pack_xyz = nullptr;
   double* d_pack_vel = nullptr;
@@ -91,9 +90,18 @@ int upload_velocities(sop_engine* e, int r, const double* vel);
 int get_rep(sop_engine* e, int r, RepDev* out);
 int put_rep(sop_engine* e, int r, const RepDev& d);
 int build_now(sop_engine* e, int r, int mode);
+int grow_rows(sop_engine* e, int r, int need);
+int rebuild_fit(sop_engine* e, int r, int mode);
 int refresh_layout(sop_engine* e);
+// batched steps inside an open run window (k_begin already issued); ms = CUDA-event time
+int run_steps(sop_engine* e, int64_t steps, float* ms);
+// open a run window of nsteps for every active replica
+int begin_all(sop_engine* e, int64_t nsteps);
+// launch-shape change: recompute the persistent grid, invalidate layout and graph
+void set_launch_shape(sop_engine* e, int threads, int chunk_beads, int stage_limit,
+                      int slice_beads);
 int enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items, int nitems,
-                 int max_n, int max_staged, int step_grid, int pro_grid);
+                 int max_staged, int step_grid, int pro_grid);
 // one step of every active replica, sized only by device-resident counts
 int enqueue_batched_step(sop_engine* e);
 int run_batched(sop_engine* e, int64_t nsteps, bool timed);

@@ -149,20 +149,17 @@ __device__ __forceinline__ void fence_async_smem() {
 }
 
 // ---------------------------------------------------------------------------------
-// K1 + K2: list build of one replica by one CTA (n <= kBuildMax)
+// K1: cell binning of one replica by one CTA into global memory (k_bin)
+// K2: neighbor/pair-list enumeration of a slice of beads (k_build units)
 
-constexpr int kWarpNat = 64;  // native partners per bead staged per warp
+constexpr int kWarpNat = 64;       // native partners per bead staged per warp
+constexpr int kStencilSlots = 128; // (2K+1)^3 <= 125 stencil cells, 4 per lane
 
 struct BuildSmem {
-  int cstart[kMaxCells + 1];
-  int ccur[kMaxCells];
   int wnat[kBuildThreads / 32][kWarpNat];
-  int wbeg[kBuildThreads / 32][32];
-  int wpre[kBuildThreads / 32][32];
-  float red[6][32];
-  int s_ok, s_nx, s_ny, s_nz, s_maxrow, s_status;
-  float s_edge, s_ox, s_oy, s_oz;
-  int s_cx0, s_cy0, s_cz0;
+  int wbeg[kBuildThreads / 32][kStencilSlots];
+  int wpre[kBuildThreads / 32][kStencilSlots];
+  int s_maxrow, s_status;
 };
 
 __device__ __forceinline__ int bsearch_sorted(const int* a, int n, int key) {
@@ -177,37 +174,40 @@ __device__ __forceinline__ int bsearch_sorted(const int* a, int n, int key) {
   return -1;
 }
 
-// Build the lists of beads [b0, b1) of replica r from position buffer `src`
-// in list mode `mode`.  Every slice bins the whole replica (O(n)) and then
-// enumerates its own beads, so slices of one replica run on different CTAs.
-// Dynamic shared memory: float4 P[n] | int sorted[n] | ushort cell[n].
-__device__ void build_lists(const DevArrays& A, int r, int src, int mode, int b0, int b1,
-                            BuildSmem& B, unsigned char* dyn) {
-  RepDev* R = &A.rep[r];
-  const int n = R->n, off = R->off, tid = threadIdx.x, nt = blockDim.x;
-  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-  float4* P = reinterpret_cast<float4*>(dyn);
-  int* sorted = reinterpret_cast<int*>(P + n);
-  unsigned short* cell = reinterpret_cast<unsigned short*>(sorted + n);
-  const float4* S = A.stage[src] + 2 * (long long)off;
-  const double* X = A.X[src];
-  const long long cap = A.cap;
-  const double boxl = R->boxl;
-  const float skin = R->skin;
-
-  // list cutoff per type pair (non-natives) and the largest one over the
-  // bead types present in this replica
+// largest non-native list cutoff over the bead types present in replica R
+__device__ __forceinline__ float list_cutoff_max(const RepDev* R, int mode) {
   float rl_max = 0.f;
   const int tmask = R->type_mask ? R->type_mask : 0x6;
   for (int a = 1; a < kMaxTypes; a++)
     for (int b = 1; b < kMaxTypes; b++) {
       if (!((tmask >> a) & 1) || !((tmask >> b) & 1)) continue;
-      float rl = (mode == SOP_LIST_SKIN) ? (float)(2.5 * c_ff.sigma_rep[a][b]) + skin
+      float rl = (mode == SOP_LIST_SKIN) ? (float)(2.5 * c_ff.sigma_rep[a][b]) + R->skin
                                          : (float)(3.2 * c_ff.sigma_rep[a][b]);
       rl_max = fmaxf(rl_max, rl);
     }
+  return rl_max;
+}
 
-  // 1. bounding box of hi positions
+// Bin replica r's beads (positions of buffer `src`) into a cell grid held in
+// global memory: relative positions + type/chain code, cell of each bead, the
+// bead ids sorted by cell (bead order within a cell) and the cell starts.
+// Cutoff modes use cells half a list cutoff wide (125-cell stencil); cell mode
+// the reference's floor(x / lcell) cells (cell_list.cpp:24-31, 27-cell
+// stencil); mode "none" one cell.  One CTA.
+__device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* smem, int smem_ints) {
+  __shared__ float red[6][32];
+  __shared__ int wsum[32];
+  __shared__ BinHdr H;
+  RepDev* R = &A.rep[r];
+  const int n = R->n, off = R->off, tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  const float4* S = A.stage[src] + 2 * (long long)off;
+  const double* X = A.X[src];
+  const long long cap = A.cap;
+  int* cst = A.cstart + R->cell_base;
+  int* ccur = A.ccur + R->cell_base;
+
+  // 1. bounding box of the hi positions
   float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
   for (int i = tid; i < n; i += nt) {
     float4 h = S[2 * i];
@@ -220,159 +220,241 @@ __device__ void build_lists(const DevArrays& A, int r, int src, int mode, int b0
       mx[c] = fmaxf(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
     }
   if (lane == 0)
-    for (int c = 0; c < 3; c++) { B.red[c][warp] = mn[c]; B.red[3 + c][warp] = mx[c]; }
+    for (int c = 0; c < 3; c++) { red[c][warp] = mn[c]; red[3 + c][warp] = mx[c]; }
   __syncthreads();
   if (tid == 0) {
     float m0[3] = {3.4e38f, 3.4e38f, 3.4e38f}, m1[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
     for (int w = 0; w < nwarp; w++)
       for (int c = 0; c < 3; c++) {
-        m0[c] = fminf(m0[c], B.red[c][w]);
-        m1[c] = fmaxf(m1[c], B.red[3 + c][w]);
+        m0[c] = fminf(m0[c], red[c][w]);
+        m1[c] = fmaxf(m1[c], red[3 + c][w]);
       }
-    int status = 0;
-    float ext = fmaxf(m1[0] - m0[0], fmaxf(m1[1] - m0[1], m1[2] - m0[2]));
+    BinHdr h;
+    h.ok = 0; h.status = 0; h.nx = h.ny = h.nz = 1; h.K = 0; h.ncell = 1;
+    h.edge = 3.0e38f; h.ox = m0[0]; h.oy = m0[1]; h.oz = m0[2]; h.cx0 = h.cy0 = h.cz0 = 0;
+    h.margin = 1e-5f;
+    const float rl_max = list_cutoff_max(R, mode);
     bool finite_box = true;
     for (int c = 0; c < 3; c++)
       finite_box = finite_box && isfinite(m0[c]) && isfinite(m1[c]) && m1[c] >= m0[c] &&
                    fabsf(m0[c]) < 1e6f && fabsf(m1[c]) < 1e6f;
     if (!finite_box) {  // non-finite or runaway positions: no grid can be built
-      B.s_status = SOP_ST_NONFINITE;
-      B.s_ok = 0;
+      h.status = SOP_ST_NONFINITE;
     } else {
-    // the minimum image must be the identity for every candidate pair
-    if ((double)ext + 2.0 * rl_max >= 0.5 * boxl) status |= SOP_ST_PERIODIC;
-    int nx, ny, nz;
-    float edge;
-    if (mode == SOP_LIST_CELL) {
-      // reference cells floor(x / lcell) (cell_list.cpp:24-31), FP64
-      double lc = R->lcell;
-      int c0[3], c1[3];
-      for (int c = 0; c < 3; c++) {
-        c0[c] = (int)floor(__ddiv_rn((double)m0[c] - 1e-3 * fabs((double)m0[c]) - 1e-3, lc));
-        c1[c] = (int)floor(__ddiv_rn((double)m1[c] + 1e-3 * fabs((double)m1[c]) + 1e-3, lc));
+      const float ext = fmaxf(m1[0] - m0[0], fmaxf(m1[1] - m0[1], m1[2] - m0[2]));
+      // the minimum image must be the identity for every candidate pair
+      if ((double)ext + 2.0 * rl_max >= 0.5 * R->boxl) h.status |= SOP_ST_PERIODIC;
+      // FP32 screening band: relative positions carry ~ext * 2^-24 of error
+      if (rl_max > 0.f) h.margin = 1e-5f + 16.0f * ext * 5.9604645e-8f / rl_max;
+      const long long ccap = R->cell_cap;
+      if (mode == SOP_LIST_CELL) {
+        const double lc = R->lcell;
+        int c0[3], c1[3];
+        for (int c = 0; c < 3; c++) {
+          c0[c] = (int)floor(__ddiv_rn((double)m0[c] - 1e-3 * fabs((double)m0[c]) - 1e-3, lc));
+          c1[c] = (int)floor(__ddiv_rn((double)m1[c] + 1e-3 * fabs((double)m1[c]) + 1e-3, lc));
+        }
+        h.cx0 = c0[0]; h.cy0 = c0[1]; h.cz0 = c0[2];
+        h.nx = c1[0] - c0[0] + 1; h.ny = c1[1] - c0[1] + 1; h.nz = c1[2] - c0[2] + 1;
+        if (2.0 * (double)(max(h.nx, max(h.ny, h.nz)) + 1) >= R->ncell) h.status |= SOP_ST_PERIODIC;
+        h.edge = (float)lc;
+        h.K = 1;
+        if ((long long)h.nx * h.ny * h.nz > ccap) h.status |= SOP_ST_GRID;
+      } else if (mode != SOP_LIST_NONE) {
+        // cells half a list cutoff wide: a 5x5x5 stencil reaches one cutoff
+        float full = fmaxf(R->cell_edge, rl_max * 1.0001f + 1e-3f);
+        for (;;) {
+          const float e = 0.5f * full;
+          const long long nx = (long long)((m1[0] - m0[0]) / e) + 1;
+          const long long ny = (long long)((m1[1] - m0[1]) / e) + 1;
+          const long long nz = (long long)((m1[2] - m0[2]) / e) + 1;
+          if (nx * ny * nz <= ccap) {
+            h.nx = (int)nx; h.ny = (int)ny; h.nz = (int)nz;
+            h.edge = e;
+            break;
+          }
+          full *= 1.25f;
+        }
+        h.K = 2;
       }
-      B.s_cx0 = c0[0]; B.s_cy0 = c0[1]; B.s_cz0 = c0[2];
-      nx = c1[0] - c0[0] + 1; ny = c1[1] - c0[1] + 1; nz = c1[2] - c0[2] + 1;
-      if (2.0 * (double)(max(nx, max(ny, nz)) + 1) >= R->ncell) status |= SOP_ST_PERIODIC;
-      edge = (float)lc;
-      if ((long long)nx * ny * nz > kMaxCells) status |= SOP_ST_GRID;
-    } else {
-      edge = (mode == SOP_LIST_NONE) ? 3.0e38f : fmaxf(R->cell_edge, rl_max * 1.0001f + 1e-3f);
-      for (;;) {
-        nx = (mode == SOP_LIST_NONE) ? 1 : (int)((m1[0] - m0[0]) / edge) + 1;
-        ny = (mode == SOP_LIST_NONE) ? 1 : (int)((m1[1] - m0[1]) / edge) + 1;
-        nz = (mode == SOP_LIST_NONE) ? 1 : (int)((m1[2] - m0[2]) / edge) + 1;
-        if ((long long)nx * ny * nz <= kMaxCells) break;
-        edge *= 1.25f;
-      }
+      h.ncell = h.nx * h.ny * h.nz;
+      h.ok = !(h.status & SOP_ST_GRID);
     }
-    B.s_status = status;
-    B.s_ok = !(status & SOP_ST_GRID) && nx >= 1 && ny >= 1 && nz >= 1;
-    B.s_nx = nx; B.s_ny = ny; B.s_nz = nz;
-    B.s_edge = edge;
-    B.s_ox = m0[0]; B.s_oy = m0[1]; B.s_oz = m0[2];
-    B.s_maxrow = 0;
-    }
+    H = h;
   }
   __syncthreads();
-  if (!B.s_ok) {
-    if (tid == 0) atomicOr(&R->status, B.s_status);
+  if (!H.ok) {
+    if (tid == 0) {
+      A.bin_hdr[r] = H;
+      atomicOr(&R->status, H.status);
+    }
     return;
   }
-  const int nx = B.s_nx, ny = B.s_ny, nz = B.s_nz, ncell = nx * ny * nz;
-  const float edge = B.s_edge, ox = B.s_ox, oy = B.s_oy, oz = B.s_oz;
+  const int nx = H.nx, ny = H.ny, nz = H.nz, ncell = H.ncell;
+  const float edge = H.edge, ox = H.ox, oy = H.oy, oz = H.oz;
 
-  // 2. relative positions (hi - origin) + lo, type|chain code, cell index
+  // working arrays (counts / starts, cursors, sorted ids) in shared memory
+  // when they fit, else directly in the replica's global bins
+  int* const gsorted = A.bin_sorted + off;
+  const bool local = 2LL * (ncell + 1) + n <= smem_ints;
+  int* const wc = local ? smem : cst;
+  int* const wq = local ? smem + ncell + 1 : ccur;
+  int* const sorted = local ? smem + 2 * (ncell + 1) : gsorted;
+
+  // 2. cell counts
+  for (int c = tid; c <= ncell; c += nt) { wc[c] = 0; wq[c] = 0; }
+  __syncthreads();
   for (int i = tid; i < n; i += nt) {
-    float4 h = S[2 * i], l = S[2 * i + 1];
+    const float4 hq = S[2 * i], lq = S[2 * i + 1];
     float4 p;
-    p.x = (h.x - ox) + l.x;
-    p.y = (h.y - oy) + l.y;
-    p.z = (h.z - oz) + l.z;
-    p.w = h.w + 4.0f * l.w;  // type + 4 * chain (exact below 2^22 chains)
-    P[i] = p;
+    p.x = (hq.x - ox) + lq.x;
+    p.y = (hq.y - oy) + lq.y;
+    p.z = (hq.z - oz) + lq.z;
+    p.w = __int_as_float((int)hq.w | ((int)lq.w << 2));  // type | chain << 2
+    A.bin_p[off + i] = p;
     int cx, cy, cz;
     if (mode == SOP_LIST_CELL) {
-      double lc = R->lcell;
-      cx = (int)floor(__ddiv_rn(X[off + i], lc)) - B.s_cx0;
-      cy = (int)floor(__ddiv_rn(X[cap + off + i], lc)) - B.s_cy0;
-      cz = (int)floor(__ddiv_rn(X[2 * cap + off + i], lc)) - B.s_cz0;
-      cx = min(max(cx, 0), nx - 1); cy = min(max(cy, 0), ny - 1); cz = min(max(cz, 0), nz - 1);
+      const double lc = R->lcell;
+      cx = (int)floor(__ddiv_rn(X[off + i], lc)) - H.cx0;
+      cy = (int)floor(__ddiv_rn(X[cap + off + i], lc)) - H.cy0;
+      cz = (int)floor(__ddiv_rn(X[2 * cap + off + i], lc)) - H.cz0;
     } else if (mode == SOP_LIST_NONE) {
       cx = cy = cz = 0;
     } else {
-      cx = min(max((int)(p.x / edge), 0), nx - 1);
-      cy = min(max((int)(p.y / edge), 0), ny - 1);
-      cz = min(max((int)(p.z / edge), 0), nz - 1);
+      cx = (int)(p.x / edge);
+      cy = (int)(p.y / edge);
+      cz = (int)(p.z / edge);
     }
-    cell[i] = (unsigned short)(cx + nx * (cy + ny * cz));
+    cx = min(max(cx, 0), nx - 1); cy = min(max(cy, 0), ny - 1); cz = min(max(cz, 0), nz - 1);
+    const int c = cx + nx * (cy + ny * cz);
+    A.bin_cell[off + i] = c;
+    atomicAdd(&wc[c], 1);
   }
-  for (int c = tid; c < ncell; c += nt) B.ccur[c] = 0;
   __syncthreads();
 
-  // 3. counting sort: per-cell counts, warp-aggregated through __match_any_sync
-  for (int base = 0; base < n; base += nt) {
-    int i = base + tid;
-    bool valid = i < n;
-    unsigned act = __ballot_sync(0xffffffffu, valid);
-    if (valid) {
-      int c = cell[i];
-      unsigned m = __match_any_sync(act, c);
-      if (lane == __ffs(m) - 1) atomicAdd(&B.ccur[c], __popc(m));
+  // 3. exclusive scan of the ncell + 1 counts (contiguous chunk per thread)
+  {
+    const int N = ncell + 1, C = (N + nt - 1) / nt, a = min(N, tid * C), b = min(N, a + C);
+    int s = 0;
+    for (int k = a; k < b; k++) s += wc[k];
+    int x = s;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
     }
-  }
-  __syncthreads();
-  // exclusive scan of counts (one warp, ncell <= kMaxCells)
-  if (warp == 0) {
-    int carry = 0;
-    for (int base = 0; base < ncell; base += 32) {
-      int c = base + lane;
-      int v = c < ncell ? B.ccur[c] : 0;
-      int x = v;
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int v = lane < nwarp ? wsum[lane] : 0, z = v;
       for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
+        const int y = __shfl_up_sync(0xffffffffu, z, o);
+        if (lane >= o) z += y;
       }
-      if (c < ncell) B.cstart[c] = carry + x - v;
-      carry += __shfl_sync(0xffffffffu, x, 31);
+      if (lane < nwarp) wsum[lane] = z - v;
     }
-    if (lane == 0) B.cstart[ncell] = carry;
-  }
-  __syncthreads();
-  for (int c = tid; c < ncell; c += nt) B.ccur[c] = 0;
-  __syncthreads();
-  // stable scatter in bead order (warp 0, 32 beads at a time)
-  if (warp == 0) {
-    for (int base = 0; base < n; base += 32) {
-      int i = base + lane;
-      bool valid = i < n;
-      unsigned act = __ballot_sync(0xffffffffu, valid);
-      int c = valid ? cell[i] : -1;
-      unsigned m = valid ? __match_any_sync(act, c) : 0u;
-      int rank = __popc(m & ((1u << lane) - 1u));
-      int basec = valid ? B.ccur[c] : 0;
-      __syncwarp();
-      if (valid) sorted[B.cstart[c] + basec + rank] = i;
-      if (valid && lane == __ffs(m) - 1) B.ccur[c] = basec + __popc(m);
-      __syncwarp();
+    __syncthreads();
+    int run = wsum[warp] + x - s;
+    for (int k = a; k < b; k++) {
+      const int v = wc[k];
+      wc[k] = run;
+      run += v;
     }
   }
   __syncthreads();
 
-  // 4. neighbor enumeration: one warp per bead; the lanes test 32 stencil
-  // candidates at a time and ballot-compact the survivors, so each row holds
-  // its partners in stencil order, bead order within a cell (deterministic).
+  // 4. scatter, then bead order inside every cell (deterministic rows)
+  if (mode == SOP_LIST_NONE) {
+    for (int i = tid; i < n; i += nt) sorted[i] = i;
+  } else {
+    for (int i = tid; i < n; i += nt) {
+      const int c = A.bin_cell[off + i];
+      sorted[wc[c] + atomicAdd(&wq[c], 1)] = i;
+    }
+    __syncthreads();
+    for (int c = tid; c < ncell; c += nt) {
+      const int a = wc[c], b = wc[c + 1];
+      for (int k = a + 1; k < b; k++) {  // insertion sort (cells hold a few beads)
+        const int v = sorted[k];
+        int m = k - 1;
+        while (m >= a && sorted[m] > v) {
+          sorted[m + 1] = sorted[m];
+          m--;
+        }
+        sorted[m + 1] = v;
+      }
+    }
+  }
+  __syncthreads();
+  if (local) {
+    for (int c = tid; c <= ncell; c += nt) cst[c] = wc[c];
+    for (int i = tid; i < n; i += nt) gsorted[i] = sorted[i];
+  }
+  if (tid == 0) {
+    A.bin_hdr[r] = H;
+    if (H.status) atomicOr(&R->status, H.status);
+  }
+}
+
+// Enumerate the list rows of beads [b0, b1) of replica r from its bins (one
+// warp per bead).  The bins are copied into shared memory when they fit in
+// `dyn_bytes`, else read from global memory (L2).  The lanes test 32
+// stencil candidates at a time and ballot-compact the survivors, so each row
+// holds its partners in stencil order, bead order within a cell.
+__device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0, int b1,
+                            BuildSmem& B, unsigned char* dyn, int dyn_bytes) {
+  RepDev* R = &A.rep[r];
+  const BinHdr H = A.bin_hdr[r];
+  if (!H.ok) return;  // k_bin recorded why
+  const int n = R->n, off = R->off, tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int nx = H.nx, ny = H.ny, nz = H.nz, ncell = H.ncell, K = H.K, SK = 2 * K + 1;
+  const int ncs = SK * SK * SK;
+  const float4* S = A.stage[src] + 2 * (long long)off;
+  const double* X = A.X[src];
+  const long long cap = A.cap;
+  const float skin = R->skin;
+
+  const float4* P = A.bin_p + off;
+  const int* sorted = A.bin_sorted + off;
+  const int* cell = A.bin_cell + off;
+  const int* cst = A.cstart + R->cell_base;
+  if ((long long)n * 24 + (long long)(ncell + 1) * 4 <= dyn_bytes) {
+    float4* Ps = reinterpret_cast<float4*>(dyn);
+    int* ss = reinterpret_cast<int*>(Ps + n);
+    int* cs = ss + n;
+    int* ts = cs + n;
+    for (int i = tid; i < n; i += nt) {
+      Ps[i] = P[i];
+      ss[i] = sorted[i];
+      cs[i] = cell[i];
+    }
+    for (int c = tid; c <= ncell; c += nt) ts[c] = cst[c];
+    __syncthreads();
+    P = Ps; sorted = ss; cell = cs; cst = ts;
+  }
+  if (tid == 0) { B.s_maxrow = 0; B.s_status = 0; }
+  __syncthreads();
+
   const long long nl_base = R->nl_base;
   const int L = R->L;
-  const float margin = 1e-5f;
+  const float margin = H.margin;
   int my_status = 0, my_max = 0;
   int* wnat = B.wnat[warp];
   int* wbeg = B.wbeg[warp];  // first sorted slot of each stencil cell
   int* wpre = B.wpre[warp];  // exclusive prefix of the stencil-cell counts
   const unsigned lt_mask = (1u << lane) - 1u;
+  const int nwarp = nt >> 5;
+  // this lane's stencil cells 4 lane + q as packed offsets (dx+K | dy+K << 4 |
+  // dz+K << 8), -1 past the stencil
+  int soff[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int k = 4 * lane + q;
+    soff[q] = k < ncs ? (k % SK) | (((k / SK) % SK) << 4) | ((k / (SK * SK)) << 8) : -1;
+  }
   for (int i = b0 + warp; i < b1; i += nwarp) {
     const float4 pi = P[i];
-    const int code_i = (int)pi.w, ti = code_i & 3, chi = code_i >> 2;
+    const int code_i = __float_as_int(pi.w), ti = code_i & 3, chi = code_i >> 2;
     const int c = cell[i];
     const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
     const int4 tp = A.topo[off + i];
@@ -385,97 +467,102 @@ __device__ void build_lists(const DevArrays& A, int r, int src, int mode, int b0
     if (nat_in_smem)
       for (int k = lane; k < nat_cnt; k += 32) wnat[k] = A.nat[tp.x + k].x & (int)kIdx;
     __syncwarp();
-    double rl2d[kMaxTypes], pl2d[kMaxTypes];
-    float rl2f[kMaxTypes], pl2f[kMaxTypes];
-    for (int t = 1; t < kMaxTypes; t++) {
-      double rl = 2.5 * c_ff.sigma_rep[ti][t] + (double)skin;
-      rl2d[t] = (mode == SOP_LIST_SKIN) ? rl * rl : c_ff.rc2_nl[ti][t];
-      rl2f[t] = (float)rl2d[t];
-      pl2d[t] = c_ff.rc2_pl[ti][t];  // (2.5 sigma)^2, sop.cpp:539-541
-      pl2f[t] = (float)pl2d[t];
-    }
-    rl2d[0] = rl2d[1];
-    rl2f[0] = rl2f[1];
-    pl2d[0] = pl2d[1];
-    pl2f[0] = pl2f[1];
-    // the 27 stencil cells (dz, dy, dx from -1 to 1) flattened into one
-    // candidate range: lane k < 27 owns cell k, a warp scan gives offsets
-    int ccount = 0, cbeg = 0;
-    if (lane < 27) {
-      const int xx = cx + lane % 3 - 1, yy = cy + (lane / 3) % 3 - 1, zz = cz + lane / 9 - 1;
-      if (xx >= 0 && xx < nx && yy >= 0 && yy < ny && zz >= 0 && zz < nz) {
-        const int cc = xx + nx * (yy + ny * zz);
-        cbeg = B.cstart[cc];
-        ccount = B.cstart[cc + 1] - cbeg;
+    // list and pair cutoffs^2 against partner types 1 and 2 (type 0 reads as 1)
+    const int tA = ti ? ti : 1;
+    const double rlA = 2.5 * c_ff.sigma_rep[tA][1] + (double)skin,
+                 rlB = 2.5 * c_ff.sigma_rep[tA][2] + (double)skin;
+    const double rl2d1 = (mode == SOP_LIST_SKIN) ? rlA * rlA : c_ff.rc2_nl[tA][1];
+    const double rl2d2 = (mode == SOP_LIST_SKIN) ? rlB * rlB : c_ff.rc2_nl[tA][2];
+    const double pl2d1 = c_ff.rc2_pl[tA][1], pl2d2 = c_ff.rc2_pl[tA][2];  // (2.5 sigma)^2, sop.cpp:539-541
+    const float rl2f1 = (float)rl2d1, rl2f2 = (float)rl2d2, pl2f1 = (float)pl2d1, pl2f2 = (float)pl2d2;
+    // the stencil cells (dz, dy, dx from -K to K) flattened into one candidate
+    // range: lane l owns stencil cells 4l..4l+3, a warp scan gives offsets
+    int cnt4[4], beg4[4], lsum = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      cnt4[q] = 0;
+      beg4[q] = 0;
+      if (soff[q] >= 0) {
+        const int xx = cx + (soff[q] & 15) - K, yy = cy + ((soff[q] >> 4) & 15) - K,
+                  zz = cz + (soff[q] >> 8) - K;
+        if (xx >= 0 && xx < nx && yy >= 0 && yy < ny && zz >= 0 && zz < nz) {
+          const int cc = xx + nx * (yy + ny * zz);
+          beg4[q] = cst[cc];
+          cnt4[q] = cst[cc + 1] - beg4[q];
+        }
       }
+      lsum += cnt4[q];
     }
-    int incl = ccount;
+    int incl = lsum;
     for (int o = 1; o < 32; o <<= 1) {
       const int y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    wbeg[lane] = cbeg;
-    wpre[lane] = incl - ccount;
+    {
+      int pre = incl - lsum;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        wbeg[4 * lane + q] = beg4[q];
+        wpre[4 * lane + q] = pre;
+        pre += cnt4[q];
+      }
+    }
     __syncwarp();
     int cnt = 0;  // warp-uniform
-    {
-      {
-        {
-          for (int base = 0; base < total; base += 32) {
-            const int f = base + lane;
-            bool pass = f < total;
-            int j = 0, tj = 1;
-            float d2 = 0.f;
-            if (pass) {
-              int lo = 0, hi = 26;  // last stencil cell whose prefix <= f
-              while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (wpre[mid] <= f) lo = mid;
-                else hi = mid - 1;
-              }
-              j = sorted[wbeg[lo] + (f - wpre[lo])];
-              const float4 pj = P[j];
-              const int code_j = (int)pj.w, chj = code_j >> 2;
-              tj = code_j & 3;
-              pass = j != i && !(chi == chj && abs(i - j) <= 2);
-              const float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
-              d2 = ddx * ddx + ddy * ddy + ddz * ddz;
-            }
-            const long long gj = off + j;
-            if (pass && mode != SOP_LIST_NONE && mode != SOP_LIST_CELL) {
-              // cell adjacency is the whole predicate in cell mode (cell_list.cpp:86-88)
-              const double rl2 = rl2d[tj];
-              pass = d2 <= rl2f[tj] * (1.0f + margin) &&
-                     within(d2, rl2f[tj], margin, [&] { return exact_d2(X, cap, gi, gj) < rl2; });
-            }
-            if (pass) {  // natives are listed separately (sorted by partner)
-              int lo = 0, hi = nat_cnt;
-              while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                const int v = nat_in_smem ? wnat[mid] : (A.nat[tp.x + mid].x & (int)kIdx);
-                if (v == j) { pass = false; break; }
-                if (v < j) lo = mid + 1;
-                else hi = mid;
-              }
-            }
-            if (pass && er.y > 0 && bsearch_sorted(A.exc + er.x, er.y, j) >= 0) pass = false;
-            bool inp = false;
-            if (pass) {
-              if (mode == SOP_LIST_NONE) {
-                inp = true;  // no pair-list filter without a cutoff type
-              } else {
-                const double rc2 = pl2d[tj];
-                inp = within(d2, pl2f[tj], margin, [&] { return exact_d2(X, cap, gi, gj) < rc2; });
-              }
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, pass);
-            const int pos = cnt + __popc(m & lt_mask);
-            if (pass && pos < L) A.nl[row + pos] = j | (inp ? (int)kPL : 0);
-            cnt += __popc(m);
-          }
+    for (int base = 0; base < total; base += 32) {
+      const int f = base + lane;
+      bool pass = f < total;
+      int j = 0, tj = 1;
+      float d2 = 0.f;
+      if (pass) {
+        int lo = 0, hi = ncs - 1;  // last stencil cell whose prefix <= f
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (wpre[mid] <= f) lo = mid;
+          else hi = mid - 1;
+        }
+        j = sorted[wbeg[lo] + (f - wpre[lo])];
+        const float4 pj = P[j];
+        const int code_j = __float_as_int(pj.w), chj = code_j >> 2;
+        tj = code_j & 3;
+        pass = j != i && !(chi == chj && abs(i - j) <= 2);
+        const float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
+        d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+      }
+      const long long gj = off + j;
+      if (pass && mode != SOP_LIST_NONE && mode != SOP_LIST_CELL) {
+        // cell adjacency is the whole predicate in cell mode (cell_list.cpp:86-88)
+        const double rl2 = tj == 2 ? rl2d2 : rl2d1;
+        const float rl2f = tj == 2 ? rl2f2 : rl2f1;
+        pass = d2 <= rl2f * (1.0f + margin) &&
+               within(d2, rl2f, margin, [&] { return exact_d2(X, cap, gi, gj) < rl2; });
+      }
+      if (pass) {  // natives are listed separately (sorted by partner)
+        int lo = 0, hi = nat_cnt;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          const int v = nat_in_smem ? wnat[mid] : (A.nat[tp.x + mid].x & (int)kIdx);
+          if (v == j) { pass = false; break; }
+          if (v < j) lo = mid + 1;
+          else hi = mid;
         }
       }
+      if (pass && er.y > 0 && bsearch_sorted(A.exc + er.x, er.y, j) >= 0) pass = false;
+      bool inp = false;
+      if (pass) {
+        if (mode == SOP_LIST_NONE) {
+          inp = true;  // no pair-list filter without a cutoff type
+        } else {
+          const double rc2 = tj == 2 ? pl2d2 : pl2d1;
+          inp = within(d2, tj == 2 ? pl2f2 : pl2f1, margin,
+                       [&] { return exact_d2(X, cap, gi, gj) < rc2; });
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, pass);
+      const int pos = cnt + __popc(m & lt_mask);
+      if (pass && pos < L) A.nl[row + pos] = j | (inp ? (int)kPL : 0);
+      cnt += __popc(m);
     }
     if (lane == 0) {
       if (cnt > L) my_status |= SOP_ST_LIST_OVERFLOW;
@@ -539,6 +626,15 @@ __device__ __forceinline__ void push_units(const DevArrays& A, int r, int kind, 
     if (base + s < A.unit_cap) A.units[base + s] = make_int4(r, kind | (mode << 8), s, buf);
 }
 
+// A list build: one binning unit for k_bin, then its slices for k_build.
+__device__ __forceinline__ void push_build(const DevArrays& A, int r, int mode, int n, int buf) {
+  A.slice_done[r] = 0;
+  A.rep[r].max_row = 0;
+  const int k = atomicAdd(A.bin_cnt, 1);
+  if (k < A.bin_cap) A.bins[k] = make_int4(r, mode, buf, 0);
+  push_units(A, r, U_BUILD, mode, (n + A.slice_beads - 1) / A.slice_beads, buf);
+}
+
 // Per-replica step bookkeeping, one thread per replica: phase, noise counter,
 // the reference's nnlup cadence or the displacement trigger, output steps.
 // Due work goes to the unit queue, in this order of meaning:
@@ -560,12 +656,9 @@ __global__ void k_decide(DevArrays A, const int* rep_ids, const int* nrep_dev, i
 __device__ void decide_one(const DevArrays& A, int r, int force_build, int build_mode) {
   RepDev* R = &A.rep[r];
   RepDev Q = *R;  // one pipelined copy; decide in registers, store back
-  const int nsl = (Q.n + kSliceBeads - 1) / kSliceBeads;
   if (force_build) {  // build_mode < 0: the replica's own list mode
-    A.slice_done[r] = 0;
-    R->max_row = 0;
     R->en_after = 0;
-    push_units(A, r, U_BUILD, build_mode >= 0 ? build_mode : Q.mode, nsl, Q.cur);
+    push_build(A, r, build_mode >= 0 ? build_mode : Q.mode, Q.n, Q.cur);
     return;
   }
   if (Q.obs_pending) {
@@ -612,24 +705,40 @@ __device__ void decide_one(const DevArrays& A, int r, int force_build, int build
   R->out = out;
   if (out) R->obs_pending = 1;
   R->en_after = need && out;
-  if (need) {
-    A.slice_done[r] = 0;
-    R->max_row = 0;
-    push_units(A, r, U_BUILD, Q.mode, nsl, prev);
-  }
+  if (need) push_build(A, r, Q.mode, Q.n, prev);
   if (out && !need) push_units(A, r, U_ENERGY, 0, 1, Q.cur);
+}
+
+// Persistent CTAs over the binning queue: one CTA bins one replica.  The last
+// CTA to exit resets the queue for the next step.
+__global__ void __launch_bounds__(kBinThreads) k_bin(DevArrays A, int dyn_bytes) {
+  extern __shared__ __align__(16) int bsm[];
+  const int cnt = min(*A.bin_cnt, A.bin_cap);
+  for (int u = blockIdx.x; u < cnt; u += gridDim.x) {
+    const int4 w = A.bins[u];
+    bin_replica(A, w.x, w.z, w.y, bsm, dyn_bytes / 4);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(A.bin_exit, 1) == (int)gridDim.x - 1) {
+      *A.bin_cnt = 0;
+      *A.bin_exit = 0;
+    }
+  }
 }
 
 // Persistent CTAs over the unit queue.  The CTA that finishes the last slice
 // of a build closes it (counters, displacement flag) and, on an output step,
 // computes the energies with the new pair list.  The last CTA to exit resets
 // the queue for the next step.
-__global__ void __launch_bounds__(kBuildThreads, 1) k_build(DevArrays A) {
+__global__ void __launch_bounds__(kBuildThreads, 1) k_build(DevArrays A, int dyn_bytes) {
   extern __shared__ __align__(16) unsigned char dyn[];
   __shared__ BuildSmem B;
   __shared__ int s_last;
   double* red = reinterpret_cast<double*>(dyn);
   const int cnt = min(*A.unit_cnt, A.unit_cap);
+  const int sb = A.slice_beads;
   for (int u = blockIdx.x; u < cnt; u += gridDim.x) {
     const int4 w = A.units[u];
     const int r = w.x, kind = w.y & 0xFF, mode = w.y >> 8;
@@ -639,9 +748,9 @@ __global__ void __launch_bounds__(kBuildThreads, 1) k_build(DevArrays A) {
     } else if (kind == U_ENERGY) {
       replica_energy(A, R, w.w, red);
     } else if (kind == U_BUILD) {
-      const int n = R->n, nsl = (n + kSliceBeads - 1) / kSliceBeads;
-      const int b0 = w.z * kSliceBeads, b1 = min(n, b0 + kSliceBeads);
-      build_lists(A, r, w.w, mode, b0, b1, B, dyn);
+      const int n = R->n, nsl = (n + sb - 1) / sb;
+      const int b0 = w.z * sb, b1 = min(n, b0 + sb);
+      build_slice(A, r, w.w, mode, b0, b1, B, dyn, dyn_bytes);
       __syncthreads();
       if (threadIdx.x == 0) {
         __threadfence();
@@ -892,6 +1001,9 @@ __global__ void __launch_bounds__(256, 3) k_step(DevArrays A, const StepItem* it
       C.amp = R->noise_amp; C.T = R->T; C.kbnd = R->kbnd; C.R0sq = R->R0sq; C.fang = R->fang;
       C.half_skin2 = R->half_skin2; C.pull_f = R->pull_f; C.pull_i = R->pull_i;
       C.pull_j = R->pull_j; C.seed_lo = R->seed_lo; C.seed_hi = R->seed_hi;
+      // a list build of this step that failed (row overflow, grid, periodic
+      // image) leaves the replica frozen: no step on incomplete lists
+      if (R->status & (SOP_ST_LIST_OVERFLOW | SOP_ST_PERIODIC | SOP_ST_GRID)) C.phase = PH_SKIP;
       sC = C;
       if (C.phase != PH_SKIP && w.staged) {
         const char* src = reinterpret_cast<const char*>(A.stage[C.cur] + 2 * (long long)C.off);
@@ -1194,24 +1306,24 @@ __global__ void k_export(DevArrays A, int r, int off, int n, int which, int capa
 // ---------------------------------------------------------------------------------
 // launchers
 
-static size_t build_dyn_smem(int max_n) {
-  size_t b = (size_t)max_n * (16 + 4 + 2) + 16, red = 4 * kBuildThreads * sizeof(double);
-  return b > red ? b : red;
-}
+static int g_build_dyn = 48 * 1024;  // k_build dynamic shared memory (set by init_kernels)
+static int g_bin_dyn = 48 * 1024;    // k_bin dynamic shared memory
 
 // Opt every kernel into the device's full per-block shared memory once.
 template <class K>
-static cudaError_t optin(K kernel, int optin_bytes) {
+static cudaError_t optin(K kernel, int optin_bytes, int* dyn_out = nullptr) {
   cudaFuncAttributes fa;
   cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
   if (e != cudaSuccess) return e;
   int dyn = optin_bytes - (int)fa.sharedSizeBytes - 1024;
+  if (dyn_out) *dyn_out = dyn;
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
 }
 
 cudaError_t init_kernels(int optin_bytes) {
   cudaError_t e;
-  if ((e = optin(k_build, optin_bytes)) != cudaSuccess) return e;
+  if ((e = optin(k_build, optin_bytes, &g_build_dyn)) != cudaSuccess) return e;
+  if ((e = optin(k_bin, optin_bytes, &g_bin_dyn)) != cudaSuccess) return e;
   if ((e = optin(k_step<1>, optin_bytes)) != cudaSuccess) return e;
   if ((e = optin(k_step<2>, optin_bytes)) != cudaSuccess) return e;
   if ((e = optin(k_step<4>, optin_bytes)) != cudaSuccess) return e;
@@ -1221,15 +1333,21 @@ cudaError_t init_kernels(int optin_bytes) {
 }
 
 cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, const int* nrep_dev,
-                            int max_n, int force_build, int build_mode, int grid, cudaStream_t s) {
+                            int force_build, int build_mode, int grid, cudaStream_t s,
+                            cudaEvent_t after_decide, cudaEvent_t after_bin) {
   if (nrep <= 0) return cudaSuccess;
   const int dgrid = (nrep + 127) / 128;
   k_decide<<<dgrid, 128, 0, s>>>(A, rep_ids, nrep_dev, nrep, force_build, build_mode);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const size_t dyn = build_dyn_smem(max_n);
+  if (after_decide && (e = cudaEventRecord(after_decide, s)) != cudaSuccess) return e;
   if (grid <= 0) grid = 1;
-  k_build<<<grid, kBuildThreads, dyn, s>>>(A);
+  k_bin<<<grid, kBinThreads, g_bin_dyn, s>>>(A, g_bin_dyn);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (after_bin && (e = cudaEventRecord(after_bin, s)) != cudaSuccess) return e;
+  // the energy / observables units use the same memory as a reduction buffer
+  const int dyn = g_build_dyn;
+  k_build<<<grid, kBuildThreads, dyn, s>>>(A, dyn);
   return cudaGetLastError();
 }
 

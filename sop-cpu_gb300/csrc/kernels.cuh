@@ -38,9 +38,30 @@ struct DevArrays {
   int* done_list;     // replicas whose run window closed (final step taken)
   int* done_cnt;
   int done_cap;
+  // cell bins of the last list build (k_bin -> k_build)
+  float4* bin_p;      // per bead: position relative to the grid origin, .w = type | chain << 2 (int bits)
+  int* bin_sorted;    // per bead slot: local bead ids sorted by cell, bead order within a cell
+  int* bin_cell;      // per bead: cell index
+  int* cstart;        // per replica cell range (RepDev::cell_base): exclusive prefix of cell counts
+  int* ccur;          // same layout: scatter cursors
+  struct BinHdr* bin_hdr;  // per replica: grid of the last binning
+  int4* bins;         // binning queue {replica, mode, buffer, 0}
+  int* bin_cnt;
+  int* bin_exit;
+  int bin_cap;
+  int slice_beads;    // beads per list-build slice unit
 };
 
-constexpr int kSliceBeads = 128;      // beads per list-build work unit
+// Grid of one replica's last binning.
+struct BinHdr {
+  int ok, status, nx, ny, nz, K, ncell;  // K: stencil half-width in cells
+  float edge, ox, oy, oz, margin;        // margin: relative FP32 screening band
+  int cx0, cy0, cz0;                     // cell-mode origin cell (floor(x / lcell))
+};
+
+constexpr int kSliceBeads = 32;       // default beads per list-build work unit
+constexpr int kMinSliceBeads = 16;
+constexpr int kMaxReplicaBeads = 1 << 22;
 
 // Work item of the step kernel: beads [b0,b1) of replica r; staged = the
 // replica's positions fit in shared memory.
@@ -49,21 +70,28 @@ struct StepItem {
 };
 
 constexpr int kStageMax = 6144;       // beads staged in shared memory (192 KB)
-constexpr int kBuildMax = 8192;       // beads per single-CTA list build
-constexpr int kMaxCells = 4096;       // cells of one list-build grid
 constexpr int kBuildThreads = 512;
+constexpr int kBinThreads = 512;
+// kernel launches of one step: k_decide, k_bin, k_build (prologue), k_step
+constexpr int kPrologueLaunches = 3;
+constexpr int kStepLaunches = 4;
+// cells a replica's binning may use (grid cells grow wider beyond that)
+inline long long cell_capacity(int n) { return 4LL * n + 4096; }
 
 void upload_tables(const FFTables& t, cudaStream_t s);
 // Opt the kernels into `optin_bytes` of shared memory per block (once per device).
 cudaError_t init_kernels(int optin_bytes);
 
-// Prologue + list build: one persistent CTA group over `nrep` replica ids.
+// Prologue + list build over `nrep` replica ids: k_decide, k_bin (one CTA per
+// replica to bin), k_build (persistent CTAs over slices, energies, observables).
 // force_build: build for every listed replica from the CURRENT buffer
 // (reference-named list updates), else the step cadence decides.
 // nrep / nitems: host counts (grid sizing); *_dev: the same counts in device
 // memory, read by the kernels when given (graphs survive layout changes).
+// after_decide / after_bin: events recorded between the three kernels (profiling)
 cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, const int* nrep_dev,
-                            int max_n, int force_build, int build_mode, int grid, cudaStream_t s);
+                            int force_build, int build_mode, int grid, cudaStream_t s,
+                            cudaEvent_t after_decide = nullptr, cudaEvent_t after_bin = nullptr);
 cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
                         int max_staged, int lanes, int threads, int grid, cudaStream_t s);
 cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s);

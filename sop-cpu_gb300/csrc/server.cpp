@@ -229,4 +229,3 @@ extern "C" int sop_server_stats(sop_server* s, int64_t* bead_steps, int* active,
   return SOP_OK;
 }
 
-extern "C" int sop_autotune(sop_engine*, int, char*, int) { return SOP_ERR_UNSUPPORTED; }

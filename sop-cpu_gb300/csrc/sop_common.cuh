@@ -44,6 +44,8 @@ struct RepDev {
   long long nl_base;       // first neighbor-list entry of the replica
   int L;                   // neighbor-list row capacity
   int nat_base, bnd_base, ang_base, exc_base;  // entry bases
+  long long cell_base;     // first cell of the replica's binning range
+  int cell_cap;            // cells the binning may use
   // configuration
   int mode;                // SOP_LIST_*
   int type_mask;           // bit t set when bead type t occurs in the replica

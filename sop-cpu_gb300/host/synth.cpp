@@ -84,19 +84,26 @@ void grow(SplitMix& rng, int n, double radius, const double* center, double* x, 
   const double b = 3.8;
   double* p = x + 3 * offset;
   if (n <= 0) return;
-  // first bead: random point inside half the sphere
-  for (;;) {
-    double v[3];
-    rng.unit(v);
-    double r = 0.5 * radius * rng.uniform();
-    for (int k = 0; k < 3; k++) p[k] = center[k] + r * v[k];
-    bool ok = true;
-    grid.near(p, [&](int j) {
-      double d2 = 0;
-      for (int k = 0; k < 3; k++) { double t = x[3 * j + k] - p[k]; d2 += t * t; }
-      if (d2 < min_sep * min_sep) ok = false;
-    });
-    if (ok) break;
+  // first bead: random point inside half the sphere, clear of earlier beads;
+  // where the region is already full, the most separated of many tries
+  {
+    double best[3] = {center[0], center[1], center[2]}, best_sep = -1.0;
+    bool ok = false;
+    for (int t = 0; t < 20000 && !ok; t++) {
+      double v[3];
+      rng.unit(v);
+      double r = 0.5 * radius * rng.uniform();
+      for (int k = 0; k < 3; k++) p[k] = center[k] + r * v[k];
+      double sep2 = 1e30;
+      grid.near(p, [&](int j) {
+        double d2 = 0;
+        for (int k = 0; k < 3; k++) { double u = x[3 * j + k] - p[k]; d2 += u * u; }
+        if (d2 < sep2) sep2 = d2;
+      });
+      ok = sep2 >= min_sep * min_sep;
+      if (!ok && sep2 > best_sep) { best_sep = sep2; std::memcpy(best, p, sizeof best); }
+    }
+    if (!ok) std::memcpy(p, best, sizeof best);
   }
   grid.insert(offset, p);
   for (int i = 1; i < n; i++) {

@@ -23,6 +23,7 @@ ERRORS = {
 ST_NONFINITE, ST_FENE, ST_LIST_OVERFLOW, ST_PERIODIC, ST_GRID = 1, 2, 4, 8, 16
 LIST_NONE, LIST_NEIGHBOR, LIST_CELL, LIST_SKIN = 0, 1, 2, 3
 TERM_RANDOM, TERM_FENE, TERM_ANGLE, TERM_VDW, TERM_ALL = 1, 2, 4, 8, 15
+TUNE_SHAPE, TUNE_LISTS = 1, 2
 PREC_MIXED, PREC_FP64 = 0, 1
 
 
@@ -72,7 +73,7 @@ class EngineConfig(C.Structure):
         ("device", C.c_int), ("max_beads", C.c_int), ("max_replicas", C.c_int),
         ("max_list_entries", C.c_int64), ("block_threads", C.c_int),
         ("lanes_per_bead", C.c_int), ("graph_steps", C.c_int),
-        ("stage_limit", C.c_int), ("chunk_beads", C.c_int),
+        ("stage_limit", C.c_int), ("chunk_beads", C.c_int), ("build_slice_beads", C.c_int),
     ]
 
 
@@ -128,7 +129,9 @@ _PROTOS = {
     "sop_run_host": (C.c_int, [VP, DP, DP, C.c_int64, DP, DP]),
     "sop_last_run_timing": (C.c_int, [VP, DP, DP, C.POINTER(C.c_int64)]),
     "sop_profile_steps": (C.c_int, [VP, C.c_int64, DP, DP]),
+    "sop_profile_steps_ex": (C.c_int, [VP, C.c_int64, DP]),
     "sop_autotune": (C.c_int, [VP, C.c_int, C.c_char_p, C.c_int]),
+    "sop_autotune_ex": (C.c_int, [VP, C.c_int, C.c_int, C.c_char_p, C.c_int]),
     "sop_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(VP)]),
     "sop_server_destroy": (C.c_int, [VP]),
     "sop_server_submit": (C.c_int, [VP, C.POINTER(SystemDesc), C.c_int64, C.POINTER(C.c_int64)]),

@@ -222,6 +222,12 @@ class Engine:
                 "sop_profile_steps")
         return s.value, p.value
 
+    def profile_split(self, nsteps: int):
+        """Mean ms per step of k_decide, k_bin, k_build and k_step (CUDA events)."""
+        out = (C.c_double * 4)()
+        L.check(L.lib().sop_profile_steps_ex(self.h, int(nsteps), out), "sop_profile_steps_ex")
+        return dict(zip(("decide", "bin", "build", "step"), list(out)))
+
     def launches(self) -> int:
         n = C.c_int64()
         L.check(L.lib().sop_engine_launches(self.h, C.byref(n)), "sop_engine_launches")
@@ -230,7 +236,11 @@ class Engine:
     def sync(self):
         L.check(L.lib().sop_engine_sync(self.h), "sop_engine_sync")
 
-    def autotune(self, steps_per_trial: int = 20) -> str:
+    def autotune(self, steps_per_trial: int = 50, shape: bool = True, lists: bool = True) -> str:
+        """Tune launch shape and/or per-size-bucket skin and cell edge; the
+        trials are real steps (see sop_autotune_ex).  Returns the trial table."""
+        what = (L.TUNE_SHAPE if shape else 0) | (L.TUNE_LISTS if lists else 0)
         buf = C.create_string_buffer(1 << 16)
-        L.check(L.lib().sop_autotune(self.h, steps_per_trial, buf, len(buf)), "sop_autotune")
+        L.check(L.lib().sop_autotune_ex(self.h, steps_per_trial, what, buf, len(buf)),
+                "sop_autotune_ex")
         return buf.value.decode()

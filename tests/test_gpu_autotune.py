@@ -1,0 +1,80 @@
+"""Autotuner (sop_autotune_ex).  Its trials are real steps of one run window:
+launch-shape tuning must leave every trajectory bit-identical to a plain
+sop_run of the same step count, and skin / cell-edge tuning must keep the
+pair list feeding each step equal to the reference's (3.2x / nnlup) pair
+sets.  Tolerances: bit-identical state for shape tuning; pair sets exact and
+positions within 1e-6 A RMSD for list tuning (row order only moves float
+rounding)."""
+import re
+
+import numpy as np
+import pytest
+
+from sop_gb300 import _lib as L
+from sop_gb300 import systems as S
+from sop_gb300.engine import Engine, make_params
+
+pytestmark = pytest.mark.gpu
+
+DET = L.TERM_FENE | L.TERM_ANGLE | L.TERM_VDW
+SIZES = [40, 90, 150, 300, 600, 1100, 1700, 2600, 5000]
+
+
+def script():
+    return [("set", "zeta", "50"), ("set", "t_step", "0.05"), ("set", "temp", "0.6"),
+            ("set", "nstep", "1000"), ("set", "nup", "1000"), ("set", "cutofftype", "neighborlist"),
+            ("set", "nnlup", "10"), ("set", "boxl", "500"), ("set", "ncell", "62.5"),
+            ("set", "run", "1")]
+
+
+def engine():
+    return Engine(0, max_beads=1 << 16, max_replicas=32, max_list_entries=1 << 24)
+
+
+def steps_of(report):
+    m = re.search(r"(\d+) trials, (\d+) steps", report)
+    assert m, report
+    return int(m.group(2))
+
+
+def pairset(ii, jj):
+    a = np.stack([np.minimum(ii, jj), np.maximum(ii, jj)], 1)
+    return a[np.lexsort((a[:, 1], a[:, 0]))]
+
+
+def test_shape_tuning_equals_plain_run():
+    systems = [S.synth_chain(8200 + k, n) for k, n in enumerate(SIZES)]
+    params = [make_params(script(), seed=4100 + k, list_mode="skin", skin=2.0)
+              for k in range(len(systems))]
+    with engine() as a:
+        ids = [a.add(s, p) for s, p in zip(systems, params)]
+        report = a.autotune(steps_per_trial=6, shape=True, lists=False)
+        total = steps_of(report)
+        want = [(a.state(r), a.energy(r), a.status(r)) for r in ids]
+    assert "chosen threads=" in report and "shape threads=" in report
+    with engine() as b:
+        ids = [b.add(s, p) for s, p in zip(systems, params)]
+        b.run(total)
+        for k, r in enumerate(ids):
+            (_, xa, va), ea, sa = want[k]
+            _, xb, vb = b.state(r)
+            np.testing.assert_array_equal(xb, xa)
+            np.testing.assert_array_equal(vb, va)
+            np.testing.assert_array_equal(b.energy(r), ea)
+            assert b.status(r) == sa and sa[0] == 0
+
+
+def test_list_tuning_keeps_reference_pair_sets():
+    system = S.synth_chain(8300, 700)
+    with engine() as e:
+        a = e.add(system, make_params(script(), force_terms=DET))  # reference cadence, untouched
+        b = e.add(system, make_params(script(), force_terms=DET, list_mode="skin", skin=2.0))
+        report = e.autotune(steps_per_trial=10, shape=False, lists=True)
+        assert "chosen bucket n=[256,1024)" in report
+        for _ in range(2):
+            for k in (2, 3):
+                np.testing.assert_array_equal(pairset(*e.pairs(a, k)), pairset(*e.pairs(b, k)))
+            xa, xb = e.state(a)[1], e.state(b)[1]
+            assert float(np.sqrt(((xa - xb) ** 2).sum(1).mean())) < 1e-6
+            assert e.status(a)[0] == 0 and e.status(b)[0] == 0
+            e.run(150)  # and the tuned list keeps tracking after the tuner

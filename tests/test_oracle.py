@@ -175,3 +175,31 @@ def test_philox_known_answers():
             (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
     for ctr, key, want in kat:
         assert tuple(O.philox(ctr, key)) == want
+
+
+@pytest.mark.parametrize("mode", ["neighborlist", "celllist"])
+def test_pruned_candidates_equal_implicit(mode):
+    """The pruned candidate set (the large-system oracle) forms the same lists,
+    forces, energies and trajectory as the full implicit set, bit for bit,
+    while no pair from beyond the pruning cutoff enters a list."""
+    system = S.synth_chain(6600, 400)
+    scr = golden_script(mode)
+    full, pruned = O.Port(), O.Port()
+    full.set_system(system)
+    # cell mode lists every candidate in adjacent 8 A cells: up to 2 sqrt(3) 8 A apart
+    pruned.set_system(system, prune=3.2 * 3.8 + 8.0 if mode == "neighborlist" else 30.0)
+    assert pruned.count("ncon_rep") < full.count("ncon_rep")
+    for p in (full, pruned):
+        for _, k, v in scr:
+            p.command(k, v)
+        p.set_force_terms(0, 1, 1, 1)
+        p.setup(True)
+    for k in range(4):  # same entries in the same order
+        np.testing.assert_array_equal(pairs(pruned, k), pairs(full, k))
+    np.testing.assert_array_equal(pruned.coords(3), full.coords(3))
+    full.run(200)
+    pruned.run(200)
+    np.testing.assert_array_equal(pruned.coords(1), full.coords(1))
+    full.energy_eval()
+    pruned.energy_eval()
+    np.testing.assert_array_equal(pruned.energies(), full.energies())
