@@ -50,7 +50,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--md-steps", type=int, default=100)
+    ap.add_argument("--md-steps", type=int, default=500)
+    ap.add_argument("--autotune", type=int, default=40,
+                    help="steps per autotuner trial during warm-up (0 = off)")
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--lo", type=int, default=30)
     ap.add_argument("--hi", type=int, default=1500)
@@ -314,6 +316,10 @@ def run_gb300(args):
     eng, ids = make_engine(systems, temps, args)
     beads = sum(s.nbead for s in systems)
     md = args.md_steps
+    tuned = None
+    if args.autotune > 0:  # its trials are real steps: part of the warm-up
+        report = eng.autotune(args.autotune)
+        tuned = [l for l in report.splitlines() if l.startswith("chosen")]
     for _ in range(args.warmup):
         eng.run(md)
     # timed: K steps, L2 flushed before each, device time by CUDA events
@@ -381,6 +387,7 @@ def run_gb300(args):
         "config": {"workload": "batched replicas: %d chains, N log-uniform %d-%d (%d beads), "
                                "T 0.4-0.9, zeta 50, dt 0.05" % (len(systems), args.lo, args.hi, beads),
                    "md_steps_per_step": md, "list_mode": args.list_mode, "skin": args.skin,
+                   "autotuned": tuned,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "flushed (256 MB write) before each timed step; working set is L2-resident within a step"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nb3 * 8,

@@ -123,6 +123,16 @@ typedef struct sop_engine_config {
                             are gathered through L1 (0 = 2048, <0 = never)    */
   int chunk_beads;       /* beads per step-kernel work item (0 = 128)          */
   int build_slice_beads; /* beads per list-build work unit, >= 16 (0 = 32)     */
+  int step_min_blocks;   /* step-kernel variant: registers sized for 2 or 3
+                            resident CTAs per SM (0 = 3)                      */
+  int step_strategy;     /* 0: CTA work items staged in shared memory; 1: warp
+                            tasks gathering through L1/L2 (same results)      */
+  int group_rebuild_pct; /* skin-mode replicas whose displacement passed this %
+                            of their trigger distance rebuild together with any
+                            replica that must, so builds cluster into fewer
+                            steps; forces and energies are exact integer sums,
+                            so trajectories do not depend on it (0 = 50,
+                            <0 = off)                                         */
 } sop_engine_config;
 
 /* ---- engine -------------------------------------------------------------- */
@@ -199,24 +209,25 @@ int sop_last_run_timing(sop_engine* e, double* total_ms, double* step_kernel_ms,
  * each kernel: mean device ms per launch of the fused step kernel and of the
  * prologue (bookkeeping + list builds + output-step energies). */
 int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_kernel_ms, double* prologue_ms);
-/* The same run split per kernel: ms[0..3] = mean k_decide, k_bin (cell
- * binning), k_build (list slices, energies, observables), k_step per step. */
+/* The same run split per kernel, mean ms per step: ms[0] launch gap before
+ * the prologue (~0), ms[1] k_prologue (bookkeeping + cell binning), ms[2]
+ * k_build (list slices, energies, observables), ms[3] k_step. */
 int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms);
 
 /* ---- autotuner --------------------------------------------------------------- */
 /* No reference counterpart.  Time the batched step of the active replicas
- * over candidate launch shapes (step-kernel block size, beads per work item,
- * shared-memory stage limit, beads per list-build slice; one choice for the
- * engine) and, for replicas in
+ * over candidate launch shapes (step strategy, stage limit, beads per work
+ * item, block size, lanes per bead, register budget, beads per list-build
+ * slice, rebuild grouping; one choice for the engine) and, for replicas in
  * skin mode, list skins and cell edges (one choice per size bucket
  * [1,256) [256,1024) [1024,4096) [4096,...)); adopt the fastest.
  * Every trial runs steps_per_trial warm-up plus steps_per_trial timed REAL
  * steps inside one run window, so the call advances each active replica
- * exactly as one sop_run of the reported step count would.  Launch-shape
- * choices leave trajectories bit-identical; skin / cell-edge choices keep the
- * pair sets exact but reorder list rows (float rounding only).  Call between
- * runs.  report (may be NULL) receives a text table of the trials.
- * sop_autotune tunes both groups. */
+ * exactly as one sop_run of the reported step count would -- bit for bit,
+ * whatever is chosen: forces and pair energies are exact fixed-point sums of
+ * their contributions and the pair filter is exact at every step, so no knob
+ * moves a trajectory.  Call between runs.  report (may be NULL) receives a
+ * text table of the trials.  sop_autotune tunes both groups. */
 #define SOP_TUNE_SHAPE 1
 #define SOP_TUNE_LISTS 2
 int sop_autotune(sop_engine* e, int steps_per_trial, char* report, int report_cap);

@@ -1,15 +1,15 @@
-// Autotuner of the batched step: launch shape (step-kernel block size, beads
-// per work item, shared-memory stage limit) for the whole engine, and list
-// parameters (skin, cell edge) per replica size bucket.
+// Autotuner of the batched step: launch shape (step strategy, stage limit,
+// beads per work item, block size, lanes per bead, register budget, build
+// slice, rebuild grouping) for the whole engine, and list parameters (skin,
+// cell edge) per replica size bucket.
 //
 // Every trial is a run of real steps: the tuner opens one run window over all
 // its trials for every active replica, so sop_autotune advances the replicas
-// exactly as one sop_run of the same number of steps would.  Launch-shape
-// knobs leave every per-bead computation unchanged (trajectories stay
-// bit-identical).  Skin and cell edge apply to replicas in skin mode only;
-// pair sets stay exact (the pair filter is exact at every step) but rows are
-// rebuilt in another order, so float summation order, and thus rounding, can
-// change.
+// exactly as one sop_run of the same number of steps would -- bit for bit,
+// whatever it chooses: every force and pair energy is an exact fixed-point
+// sum of its contributions, so neither list order, build times, lane count
+// nor the kernel variant moves a trajectory, and the pair filter is exact at
+// every step whatever the skin or cell edge.
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
@@ -28,10 +28,6 @@ using namespace sop;
   } while (0)
 
 namespace {
-
-struct Shape {
-  int threads, chunk, stage, slice;
-};
 
 struct Bucket {
   int lo, hi;
@@ -119,10 +115,24 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
 
   // candidates
   const int stage_max = std::min<int>(kStageMax, ((int)e->prop.sharedMemPerBlockOptin - 1024) / 32);
-  std::vector<int> stages, chunks = {64, 128, 256, 512}, threads = {64, 128, 256},
-                   slices = {16, 32, 64, 128};
+  std::vector<int> stages;
   for (int s : {-1, 1024, 2048, 4096})
     if (s <= stage_max) stages.push_back(s);
+  struct Knob {
+    const char* name;
+    int LaunchShape::*field;
+    std::vector<int> values;
+  };
+  const std::vector<Knob> knobs = {
+      {"warp", &LaunchShape::strategy, {0, 1}},
+      {"stage", &LaunchShape::stage, stages},
+      {"chunk", &LaunchShape::chunk, {64, 128, 256, 512}},
+      {"threads", &LaunchShape::threads, {64, 128, 256}},
+      {"lanes", &LaunchShape::lanes, {1, 2, 4}},
+      {"occ", &LaunchShape::min_blocks, {2, 3}},
+      {"slice", &LaunchShape::slice, {16, 32, 64, 128}},
+      {"group", &LaunchShape::group_pct, {0, 30, 50, 70}},
+  };
   const std::vector<double> skins = {1.0, 1.5, 2.0, 3.0, 4.0};
   const std::vector<double> edge_pads = {0.0, 2.0, 4.0};
   std::vector<Bucket> buckets = {{1, 256, {}}, {256, 1024, {}}, {1024, 4096, {}}, {4096, 1 << 30, {}}};
@@ -137,44 +147,43 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
   buckets.erase(std::remove_if(buckets.begin(), buckets.end(), [](const Bucket& b) { return b.ids.empty(); }),
                 buckets.end());
 
-  // trials: one baseline, then every other value of each knob in turn
+  // trials: one baseline, then every value of each knob in turn
   int ntrials = 1;
   if (what & SOP_TUNE_SHAPE)
-    ntrials += (int)(stages.size() + chunks.size() + threads.size() + slices.size());
+    for (const Knob& k : knobs) ntrials += (int)k.values.size();
   for (size_t b = 0; b < buckets.size(); b++) ntrials += (int)(skins.size() + edge_pads.size());
   Tuner T{e, steps_per_trial, (int64_t)ntrials * 2 * steps_per_trial, std::string()};
   const int64_t total = T.left;
   rc = begin_all(e, total);
   if (rc) return rc;
 
-  Shape cur{e->cfg.block_threads, e->cfg.chunk_beads, e->cfg.stage_limit > 0 ? e->cfg.stage_limit : -1,
-            e->cfg.build_slice_beads};
+  auto describe = [](const LaunchShape& s) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "threads=%d chunk=%d stage=%d slice=%d occ=%d warp=%d lanes=%d group=%d",
+             s.threads, s.chunk, s.stage, s.slice, s.min_blocks, s.strategy, s.lanes, s.group_pct);
+    return std::string(buf);
+  };
+  LaunchShape cur = get_launch_shape(e);
   double best = 0;
   rc = T.trial(&best);
   if (rc) return rc;
-  T.note("baseline threads=%d chunk=%d stage=%d slice=%d  %.4f ms/step\n", cur.threads, cur.chunk,
-         cur.stage, cur.slice, best);
+  T.note("baseline %s  %.4f ms/step\n", describe(cur).c_str(), best);
   int used = 1;
-
-  auto try_shape = [&](Shape s) -> int {
-    set_launch_shape(e, s.threads, s.chunk, s.stage, s.slice);
-    double ms = 0;
-    int r2 = T.trial(&ms);
-    if (r2) return r2;
-    used++;
-    T.note("shape threads=%d chunk=%d stage=%d slice=%d  %.4f ms/step\n", s.threads, s.chunk,
-           s.stage, s.slice, ms);
-    if (ms < best * 0.99) { best = ms; cur = s; }
-    set_launch_shape(e, cur.threads, cur.chunk, cur.stage, cur.slice);
-    return SOP_OK;
-  };
   if (what & SOP_TUNE_SHAPE) {
     // each knob sweeps its values with the others at their best so far; a
     // knob's current value is re-timed once so the comparison is fresh
-    for (int s : stages) { Shape c = cur; c.stage = s; if ((rc = try_shape(c))) return rc; }
-    for (int c : chunks) { Shape x = cur; x.chunk = c; if ((rc = try_shape(x))) return rc; }
-    for (int t : threads) { Shape x = cur; x.threads = t; if ((rc = try_shape(x))) return rc; }
-    for (int q : slices) { Shape x = cur; x.slice = q; if ((rc = try_shape(x))) return rc; }
+    for (const Knob& k : knobs)
+      for (int v : k.values) {
+        LaunchShape s = cur;
+        s.*(k.field) = v;
+        set_launch_shape(e, s);
+        double ms = 0;
+        if ((rc = T.trial(&ms))) return rc;
+        used++;
+        T.note("shape %s  %.4f ms/step\n", describe(s).c_str(), ms);
+        if (ms < best * 0.99) { best = ms; cur = s; }
+        set_launch_shape(e, cur);
+      }
   }
 
   const FFTables& F = tables();
@@ -217,8 +226,8 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
   float ms = 0;
   rc = run_steps(e, T.left + 1, &ms);
   if (rc) return rc;
-  T.note("chosen threads=%d chunk=%d stage=%d slice=%d  %.4f ms/step; %d trials, %lld steps\n",
-         cur.threads, cur.chunk, cur.stage, cur.slice, best, used, (long long)total);
+  T.note("chosen %s  %.4f ms/step; %d trials, %lld steps\n", describe(cur).c_str(), best, used,
+         (long long)total);
   if (report && report_cap > 0) {
     std::strncpy(report, T.log.c_str(), report_cap - 1);
     report[report_cap - 1] = 0;

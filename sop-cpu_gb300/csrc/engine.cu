@@ -191,6 +191,8 @@ extern "C" void sop_engine_config_default(sop_engine_config* c) {
   c->stage_limit = 2048;
   c->chunk_beads = 128;
   c->build_slice_beads = kSliceBeads;
+  c->step_min_blocks = 3;
+  c->group_rebuild_pct = 50;
 }
 
 // ---- engine lifetime ------------------------------------------------------------
@@ -216,7 +218,13 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
     if (cfg_in->stage_limit != 0) cfg.stage_limit = cfg_in->stage_limit;
     if (cfg_in->chunk_beads > 0) cfg.chunk_beads = cfg_in->chunk_beads;
     if (cfg_in->build_slice_beads > 0) cfg.build_slice_beads = cfg_in->build_slice_beads;
+    if (cfg_in->step_min_blocks > 0) cfg.step_min_blocks = cfg_in->step_min_blocks;
+    if (cfg_in->step_strategy > 0) cfg.step_strategy = cfg_in->step_strategy;
+    if (cfg_in->group_rebuild_pct != 0) cfg.group_rebuild_pct = cfg_in->group_rebuild_pct;
   }
+  if (cfg.group_rebuild_pct < 0 || cfg.group_rebuild_pct >= 100) cfg.group_rebuild_pct = 0;
+  if (cfg.step_strategy != 1) cfg.step_strategy = 0;
+  if (cfg.step_min_blocks != 2) cfg.step_min_blocks = 3;
   if (cfg.stage_limit > kStageMax) cfg.stage_limit = kStageMax;
   if (cfg.chunk_beads < 32) cfg.chunk_beads = 32;
   if (cfg.build_slice_beads < kMinSliceBeads) cfg.build_slice_beads = kMinSliceBeads;
@@ -265,6 +273,14 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(dalloc(&A.pairs_out, e->pairs_cap));
   CK(dalloc(&A.pairs_cnt, 1));
   CK(dalloc(&A.err, 1));
+  CK(dalloc(&A.step_ctr, 3));
+  CK(cudaMemsetAsync(A.step_ctr, 0, 3 * sizeof(int), e->stream));
+  A.any_rebuild = A.step_ctr + 2;
+  // grouped skin rebuilds: replicas past this fraction of their trigger
+  // distance rebuild together with one that must (0 = off)
+  A.group_frac2 = cfg.group_rebuild_pct > 0
+                      ? (float)(0.01 * cfg.group_rebuild_pct * 0.01 * cfg.group_rebuild_pct)
+                      : 4.0f;
   CK(cudaMemsetAsync(A.err, 0, sizeof(int), e->stream));
   // unit queue: every replica may queue all its build slices plus two units
   A.slice_beads = cfg.build_slice_beads;
@@ -290,11 +306,6 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(dalloc(&A.cstart, cellcap));
   CK(dalloc(&A.ccur, cellcap));
   CK(dalloc(&A.bin_hdr, cfg.max_replicas));
-  A.bin_cap = cfg.max_replicas;
-  CK(dalloc(&A.bins, A.bin_cap));
-  CK(dalloc(&A.bin_cnt, 2));
-  A.bin_exit = A.bin_cnt + 1;
-  CK(cudaMemsetAsync(A.bin_cnt, 0, 2 * sizeof(int), e->stream));
   e->cells.init(cellcap);
   CK(dalloc(&e->d_ids, cfg.max_replicas + 4));
   CK(dalloc(&e->d_items, cap / 32 + cfg.max_replicas + 16));
@@ -309,7 +320,7 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   e->reps.resize(cfg.max_replicas);
   upload_tables(tables(), e->stream);
   CK(cudaGetLastError());
-  CK(init_kernels((int)e->prop.sharedMemPerBlockOptin));
+  CK(init_kernels((int)e->prop.sharedMemPerBlockOptin, (int)e->prop.sharedMemPerMultiprocessor));
   CK(dalloc(&e->d_counts, 2));
   CK(cudaMemsetAsync(e->d_counts, 0, 2 * sizeof(int), e->stream));
   CK(dalloc(&e->d_pack_xyz, 3 * cap));
@@ -319,7 +330,8 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   // fixed launch shapes of the batched step (so captured graphs stay valid):
   // persistent step CTAs as many as fit, staging sized by the stage limit
   e->max_staged = cfg.stage_limit > 0 ? cfg.stage_limit : 0;
-  e->step_grid = step_blocks_per_sm(cfg.lanes_per_bead, cfg.block_threads, e->max_staged) *
+  e->step_grid = step_blocks_per_sm(cfg.lanes_per_bead, cfg.step_min_blocks, cfg.step_strategy, cfg.block_threads,
+                                    e->max_staged) *
                  e->prop.multiProcessorCount;
   e->pro_grid = 2 * e->prop.multiProcessorCount;  // k_build CTAs over the unit queue
   for (int k = 0; k < 4; k++) CK(cudaEventCreate(&e->ev[k]));
@@ -339,7 +351,7 @@ extern "C" int sop_engine_destroy(sop_engine* e) {
                   A.rep, A.pairs_out, A.pairs_cnt, A.err, A.units, A.unit_cnt, A.slice_done,
                   A.done_list, A.done_cnt, e->d_ids, e->d_items, e->d_counts, e->d_pack_xyz,
                   e->d_pack_vel, e->d_pack_ids, e->d_pack_off, A.bin_p, A.bin_sorted,
-                  A.bin_cell, A.cstart, A.ccur, A.bin_hdr, A.bins, A.bin_cnt};
+                  A.bin_cell, A.cstart, A.ccur, A.bin_hdr, A.step_ctr};
   for (void* p : ptrs) cudaFree(p);
   if (e->h_rep) cudaFreeHost(e->h_rep);
   for (int k = 0; k < 4; k++) if (e->ev[k]) cudaEventDestroy(e->ev[k]);
@@ -382,6 +394,7 @@ static int fill_repdev(const sop_params& p, RepDev& d) {
   if (p.T < kEpsT && p.T != 0.0) d.T = 0.0f;  // keep the sop.cpp:316 branch exact
   d.kbnd = (float)p.k_bnd;
   d.R0sq = (float)(p.R0 * p.R0);
+  d.inv_R0sq = (float)(1.0 / (p.R0 * p.R0));
   d.kbnd_d = p.k_bnd;
   d.R0sq_d = p.R0 * p.R0;
   double s6 = std::pow(p.sigma_ss, 6.0);
@@ -622,8 +635,9 @@ int sop::upload_positions(sop_engine* e, int r, const double* xyz, int which_buf
     for (int c = 0; c < 3; c++) soa[(size_t)c * n + i] = xyz[3 * i + c];
     float h[3], l[3];
     for (int c = 0; c < 3; c++) split_double(xyz[3 * i + c], h[c], l[c]);
-    st[2 * i] = make_float4(h[0], h[1], h[2], (float)R.type[i]);
-    st[2 * i + 1] = make_float4(l[0], l[1], l[2], (float)R.chain[i]);
+    // .w: bead type and chain id as integer bits
+    st[2 * i] = make_float4(h[0], h[1], h[2], u2f((uint32_t)R.type[i]));
+    st[2 * i + 1] = make_float4(l[0], l[1], l[2], u2f((uint32_t)R.chain[i]));
   }
   for (int b = 0; b < 2; b++) {
     if (!(which_bufs & (1 << b))) continue;
@@ -877,6 +891,7 @@ extern "C" int sop_replica_set_params(sop_engine* e, int r, const sop_params* p)
   d.a1 = cfg.a1; d.a2 = cfg.a2; d.a3 = cfg.a3; d.a4 = cfg.a4;
   d.a1d = cfg.a1d; d.a2d = cfg.a2d; d.a3d = cfg.a3d; d.a4d = cfg.a4d;
   d.noise_amp = cfg.noise_amp; d.T = cfg.T; d.kbnd = cfg.kbnd; d.R0sq = cfg.R0sq;
+  d.inv_R0sq = cfg.inv_R0sq;
   d.kbnd_d = cfg.kbnd_d; d.R0sq_d = cfg.R0sq_d; d.fang = cfg.fang; d.fang_d = cfg.fang_d;
   d.e_bnd_coeff = cfg.e_bnd_coeff; d.e_ang_coeff = cfg.e_ang_coeff; d.pull_f = cfg.pull_f;
   d.seed_lo = cfg.seed_lo; d.seed_hi = cfg.seed_hi;
@@ -1027,18 +1042,18 @@ int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem*
                       int nitems, int max_staged, int step_grid, int pro_grid) {
   CK(launch_prologue(e->A, d_ids, nrep, nullptr, 0, 0, pro_grid, e->stream));
   CK(launch_step(e->A, d_items, nitems, nullptr, max_staged, e->cfg.lanes_per_bead,
-                 e->cfg.block_threads, step_grid, e->stream));
+                 e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads, step_grid, e->stream));
   e->launches += kStepLaunches;
   return SOP_OK;
 }
 
-// One batched step: k_decide, k_bin + k_build (builds, energies, observables),
+// One batched step: k_prologue (bookkeeping, binning), k_build (list slices, energies, observables),
 // k_step, sized by the engine's fixed grids and the device-resident counts.
 int sop::enqueue_batched_step(sop_engine* e) {
   CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0,
                      e->pro_grid, e->stream));
   CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, e->max_staged,
-                 e->cfg.lanes_per_bead, e->cfg.block_threads, e->step_grid, e->stream));
+                 e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads, e->step_grid, e->stream));
   e->launches += kStepLaunches;
   return SOP_OK;
 }
@@ -1239,18 +1254,38 @@ int sop::run_steps(sop_engine* e, int64_t steps, float* ms) {
   return check_errors(e);
 }
 
-void sop::set_launch_shape(sop_engine* e, int threads, int chunk_beads, int stage_limit,
-                           int slice_beads) {
-  e->cfg.block_threads = threads;
-  e->cfg.build_slice_beads = std::max(slice_beads, kMinSliceBeads);
+sop::LaunchShape sop::get_launch_shape(const sop_engine* e) {
+  LaunchShape s;
+  s.threads = e->cfg.block_threads;
+  s.chunk = e->cfg.chunk_beads;
+  s.stage = e->cfg.stage_limit > 0 ? e->cfg.stage_limit : -1;
+  s.slice = e->cfg.build_slice_beads;
+  s.min_blocks = e->cfg.step_min_blocks;
+  s.strategy = e->cfg.step_strategy;
+  s.lanes = e->cfg.lanes_per_bead;
+  s.group_pct = e->cfg.group_rebuild_pct;
+  return s;
+}
+
+void sop::set_launch_shape(sop_engine* e, const LaunchShape& s) {
+  e->cfg.block_threads = s.threads;
+  e->cfg.step_strategy = s.strategy == 1 ? 1 : 0;
+  e->cfg.step_min_blocks = s.min_blocks == 2 ? 2 : 3;
+  e->cfg.lanes_per_bead = s.lanes;
+  e->cfg.build_slice_beads = std::max(s.slice, kMinSliceBeads);
   e->A.slice_beads = e->cfg.build_slice_beads;
-  e->cfg.chunk_beads = chunk_beads;
-  e->cfg.stage_limit = std::min(stage_limit, kStageMax);
+  e->cfg.chunk_beads = s.chunk;
+  e->cfg.stage_limit = std::min(s.stage, kStageMax);
   e->max_staged = e->cfg.stage_limit > 0 ? e->cfg.stage_limit : 0;
-  e->step_grid = std::max(1, step_blocks_per_sm(e->cfg.lanes_per_bead, threads, e->max_staged)) *
+  e->cfg.group_rebuild_pct = (s.group_pct > 0 && s.group_pct < 100) ? s.group_pct : 0;
+  e->A.group_frac2 = e->cfg.group_rebuild_pct > 0
+                         ? (float)(1e-4 * e->cfg.group_rebuild_pct * e->cfg.group_rebuild_pct)
+                         : 4.0f;
+  e->step_grid = std::max(1, step_blocks_per_sm(e->cfg.lanes_per_bead, e->cfg.step_min_blocks,
+                                                   e->cfg.step_strategy, s.threads, e->max_staged)) *
                  e->prop.multiProcessorCount;
   e->layout_dirty = true;
-  e->graph_valid = false;
+  e->graph_valid = false;  // kernels take the device arrays by value
 }
 
 extern "C" int sop_run(sop_engine* e, int64_t nsteps) {
@@ -1278,7 +1313,7 @@ extern "C" int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms) {
   k_begin<<<(nrep + 127) / 128, 128, 0, e->stream>>>(e->A.rep, e->d_ids, nrep, nsteps);
   e->launches++;
   const int64_t iters = nsteps + 1;
-  constexpr int kE = 5;  // before k_decide, after k_decide, after k_bin, after k_build, after k_step
+  constexpr int kE = 5;  // event marks: start, before k_prologue, after it, after k_build, after k_step
   std::vector<cudaEvent_t> ev(kE * iters);
   for (auto& x : ev) CK(cudaEventCreate(&x));
   for (int64_t s = 0; s < iters; s++) {
@@ -1288,7 +1323,7 @@ extern "C" int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms) {
                        e->stream, E[1], E[2]));
     CK(cudaEventRecord(E[3], e->stream));
     CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, e->max_staged,
-                   e->cfg.lanes_per_bead, e->cfg.block_threads, e->step_grid, e->stream));
+                   e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads, e->step_grid, e->stream));
     CK(cudaEventRecord(E[4], e->stream));
     e->launches += kStepLaunches;
   }
@@ -1409,7 +1444,7 @@ static int run_phase(sop_engine* e, int r, int phase) {
   CK(h2d(e->d_items + item_slot, items.data(), items.size(), e->stream));
   k_set_phase<<<1, 1, 0, e->stream>>>(e->A.rep, r, phase);
   CK(launch_step(e->A, e->d_items + item_slot, (int)items.size(), nullptr, staged ? R.n : 0,
-                 e->cfg.lanes_per_bead, e->cfg.block_threads,
+                 e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads,
                  std::min((int)items.size(), 4 * e->prop.multiProcessorCount), e->stream));
   e->launches += 2;
   CK(cudaStreamSynchronize(e->stream));

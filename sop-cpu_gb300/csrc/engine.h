@@ -97,9 +97,20 @@ int refresh_layout(sop_engine* e);
 int run_steps(sop_engine* e, int64_t steps, float* ms);
 // open a run window of nsteps for every active replica
 int begin_all(sop_engine* e, int64_t nsteps);
-// launch-shape change: recompute the persistent grid, invalidate layout and graph
-void set_launch_shape(sop_engine* e, int threads, int chunk_beads, int stage_limit,
-                      int slice_beads);
+// Knobs that change how the batched step is launched but not what it computes.
+struct LaunchShape {
+  int threads;     // step-kernel block size
+  int chunk;       // beads per step work item
+  int stage;       // stage limit (beads; -1 = never staged)
+  int slice;       // beads per list-build slice
+  int min_blocks;  // step-kernel register budget: 2 or 3 CTAs per SM
+  int strategy;    // 0 CTA items, 1 warp tasks
+  int lanes;       // lanes per bead
+  int group_pct;   // grouped skin rebuilds (0 = off)
+};
+LaunchShape get_launch_shape(const sop_engine* e);
+// recompute the persistent grid, invalidate layout and graph
+void set_launch_shape(sop_engine* e, const LaunchShape& s);
 int enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items, int nitems,
                  int max_staged, int step_grid, int pro_grid);
 // one step of every active replica, sized only by device-resident counts

@@ -1,25 +1,29 @@
 // GB300 kernels of the SOP hot path.
 //
-//   k_decide    per-replica step bookkeeping (phase, noise counter, the
+//   k_prologue  K0 per-replica step bookkeeping (phase, noise counter, the
 //               reference's nnlup cadence or the displacement trigger) that
-//               queues the step's due work units.
-//   k_build     persistent CTAs over those units: list builds in 128-bead
-//               slices -- K1 cell binning (warp-match counting sort, stable by
-//               bead) and K2 neighbor/pair-list build over the 27-cell stencil,
-//               one warp per bead, cutoffs decided bit-exactly against the
-//               reference's FP64 arithmetic -- and output-step energies and
+//               queues the step's due work units, and K1 the cell binning of
+//               every replica whose lists are rebuilt this step (one CTA per
+//               replica: shared-memory counting sort into global bins, bead
+//               order within a cell).
+//   k_build     persistent CTAs over those units: K2 neighbor/pair-list
+//               enumeration in slices of beads over the binned stencil, one
+//               warp per bead, cutoffs decided bit-exactly against the
+//               reference's FP64 arithmetic; output-step energies and
 //               observables.
 //   k_step      K3+K4 fused: pair/bond/angle forces in FP32 from positions
 //               staged in shared memory by TMA bulk copies, lane partials to
 //               int64 fixed point and reduced with warp shuffles, counter-
 //               based Langevin noise drawn in-kernel, the underdamped update
 //               with FP64 position accumulation, next step's pair-list bits.
+//   k_step_w    the same step with warps as independent workers over L1/L2.
 //   k_energy    K5 energy terms in FP64 with a fixed-order reduction.
 //   k_obs       K6 observables (Q, Rg^2, kinT) in FP64.
 //   k_pairlist  update_pair_list at the current positions.
 //   k_export    pair lists as (i<j) pairs for checking.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "../../include/sop_gpu.h"
@@ -149,7 +153,7 @@ __device__ __forceinline__ void fence_async_smem() {
 }
 
 // ---------------------------------------------------------------------------------
-// K1: cell binning of one replica by one CTA into global memory (k_bin)
+// K1: cell binning of one replica by one CTA into global memory (k_prologue)
 // K2: neighbor/pair-list enumeration of a slice of beads (k_build units)
 
 constexpr int kWarpNat = 64;       // native partners per bead staged per warp
@@ -310,7 +314,7 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
     p.x = (hq.x - ox) + lq.x;
     p.y = (hq.y - oy) + lq.y;
     p.z = (hq.z - oz) + lq.z;
-    p.w = __int_as_float((int)hq.w | ((int)lq.w << 2));  // type | chain << 2
+    p.w = u2f(f2u(hq.w) | (f2u(lq.w) << 2));  // type | chain << 2
     A.bin_p[off + i] = p;
     int cx, cy, cz;
     if (mode == SOP_LIST_CELL) {
@@ -404,7 +408,7 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
                             BuildSmem& B, unsigned char* dyn, int dyn_bytes) {
   RepDev* R = &A.rep[r];
   const BinHdr H = A.bin_hdr[r];
-  if (!H.ok) return;  // k_bin recorded why
+  if (!H.ok) return;  // the binning recorded why
   const int n = R->n, off = R->off, tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int nx = H.nx, ny = H.ny, nz = H.nz, ncell = H.ncell, K = H.K, SK = 2 * K + 1;
@@ -616,7 +620,7 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
 __device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* red);
 __device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red);
 
-// Work units queued by k_decide for k_build: {replica, kind | mode << 8, slice, buffer}.
+// Work units queued by k_prologue for k_build: {replica, kind | mode << 8, slice, buffer}.
 enum UnitKind : int { U_OBS = 1, U_BUILD = 2, U_ENERGY = 3 };
 
 __device__ __forceinline__ void push_units(const DevArrays& A, int r, int kind, int mode, int nsl,
@@ -626,12 +630,10 @@ __device__ __forceinline__ void push_units(const DevArrays& A, int r, int kind, 
     if (base + s < A.unit_cap) A.units[base + s] = make_int4(r, kind | (mode << 8), s, buf);
 }
 
-// A list build: one binning unit for k_bin, then its slices for k_build.
+// A list build's slices for k_build (its binning is done by k_prologue).
 __device__ __forceinline__ void push_build(const DevArrays& A, int r, int mode, int n, int buf) {
   A.slice_done[r] = 0;
   A.rep[r].max_row = 0;
-  const int k = atomicAdd(A.bin_cnt, 1);
-  if (k < A.bin_cap) A.bins[k] = make_int4(r, mode, buf, 0);
   push_units(A, r, U_BUILD, mode, (n + A.slice_beads - 1) / A.slice_beads, buf);
 }
 
@@ -642,24 +644,16 @@ __device__ __forceinline__ void push_build(const DevArrays& A, int r, int mode, 
 //   the list build from X_{t-1} in slices (sop.cpp:156-170: rebuild before the step),
 //   the energies of this output step at X_t with pair list PL_t (after the build,
 //   before the step kernel rewrites the pair-list bits).
-__device__ void decide_one(const DevArrays& A, int r, int force_build, int build_mode);
-
-// nrep comes from device memory when nrep_dev is set, so a captured graph
-// keeps working when replicas are admitted or retired.
-__global__ void k_decide(DevArrays A, const int* rep_ids, const int* nrep_dev, int nrep_host,
-                         int force_build, int build_mode) {
-  const int nrep = nrep_dev ? *nrep_dev : nrep_host;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nrep; k += gridDim.x * blockDim.x)
-    decide_one(A, rep_ids[k], force_build, build_mode);
-}
-
-__device__ void decide_one(const DevArrays& A, int r, int force_build, int build_mode) {
+// Returns -1, or the build due now as mode | buffer << 8.
+// group: some replica's displacement trigger fired in the last step.
+__device__ int decide_one(const DevArrays& A, int r, int force_build, int build_mode, int group) {
   RepDev* R = &A.rep[r];
   RepDev Q = *R;  // one pipelined copy; decide in registers, store back
   if (force_build) {  // build_mode < 0: the replica's own list mode
+    const int mode = build_mode >= 0 ? build_mode : Q.mode;
     R->en_after = 0;
-    push_build(A, r, build_mode >= 0 ? build_mode : Q.mode, Q.n, Q.cur);
-    return;
+    push_build(A, r, mode, Q.n, Q.cur);
+    return mode | (Q.cur << 8);
   }
   if (Q.obs_pending) {
     push_units(A, r, U_OBS, 0, 1, Q.cur);
@@ -669,7 +663,7 @@ __device__ void decide_one(const DevArrays& A, int r, int force_build, int build
       (Q.status & (SOP_ST_NONFINITE | SOP_ST_LIST_OVERFLOW | SOP_ST_PERIODIC | SOP_ST_GRID))) {
     R->phase = PH_SKIP;
     R->out = 0;
-    return;
+    return -1;
   }
   bool need = false;
   const int prev = Q.cur;
@@ -680,7 +674,8 @@ __device__ void decide_one(const DevArrays& A, int r, int force_build, int build
       Q.inlup++;
       R->inlup = Q.inlup;
     } else if (Q.mode == SOP_LIST_SKIN) {
-      need = Q.rebuild != 0;
+      // its own trigger, or another replica's while this one is near its own
+      need = Q.rebuild != 0 || (group && Q.near != 0);
     }
     Q.cur ^= 1;
     Q.moved = 0;
@@ -707,24 +702,29 @@ __device__ void decide_one(const DevArrays& A, int r, int force_build, int build
   R->en_after = need && out;
   if (need) push_build(A, r, Q.mode, Q.n, prev);
   if (out && !need) push_units(A, r, U_ENERGY, 0, 1, Q.cur);
+  return need ? (Q.mode | (prev << 8)) : -1;
 }
 
-// Persistent CTAs over the binning queue: one CTA bins one replica.  The last
-// CTA to exit resets the queue for the next step.
-__global__ void __launch_bounds__(kBinThreads) k_bin(DevArrays A, int dyn_bytes) {
+// K0 + K1: the step bookkeeping of every listed replica and, for those that
+// rebuild their lists this step, the cell binning; persistent CTAs, one
+// replica at a time (thread 0 decides, the CTA bins).  nrep comes from device
+// memory when nrep_dev is set, so a captured graph keeps working when
+// replicas are admitted or retired.
+__global__ void __launch_bounds__(kBinThreads, 2) k_prologue(DevArrays A, const int* rep_ids,
+                                                            const int* nrep_dev, int nrep_host,
+                                                            int force_build, int build_mode,
+                                                            int dyn_bytes) {
   extern __shared__ __align__(16) int bsm[];
-  const int cnt = min(*A.bin_cnt, A.bin_cap);
-  for (int u = blockIdx.x; u < cnt; u += gridDim.x) {
-    const int4 w = A.bins[u];
-    bin_replica(A, w.x, w.z, w.y, bsm, dyn_bytes / 4);
+  __shared__ int s_build;
+  const int nrep = nrep_dev ? *nrep_dev : nrep_host;
+  const int group = *A.any_rebuild;  // cleared by k_build, after every CTA here read it
+  for (int k = blockIdx.x; k < nrep; k += gridDim.x) {
+    const int r = rep_ids[k];
+    if (threadIdx.x == 0) s_build = decide_one(A, r, force_build, build_mode, group);
     __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(A.bin_exit, 1) == (int)gridDim.x - 1) {
-      *A.bin_cnt = 0;
-      *A.bin_exit = 0;
-    }
+    const int b = s_build;
+    if (b >= 0) bin_replica(A, r, b >> 8, b & 0xFF, bsm, dyn_bytes / 4);
+    __syncthreads();
   }
 }
 
@@ -732,13 +732,15 @@ __global__ void __launch_bounds__(kBinThreads) k_bin(DevArrays A, int dyn_bytes)
 // of a build closes it (counters, displacement flag) and, on an output step,
 // computes the energies with the new pair list.  The last CTA to exit resets
 // the queue for the next step.
-__global__ void __launch_bounds__(kBuildThreads, 1) k_build(DevArrays A, int dyn_bytes) {
+__global__ void __launch_bounds__(kBuildThreads, 2) k_build(DevArrays A, int dyn_bytes) {
   extern __shared__ __align__(16) unsigned char dyn[];
   __shared__ BuildSmem B;
   __shared__ int s_last;
   double* red = reinterpret_cast<double*>(dyn);
   const int cnt = min(*A.unit_cnt, A.unit_cap);
   const int sb = A.slice_beads;
+  // the grouped-rebuild signal of the last step has been read by k_prologue
+  if (blockIdx.x == 0 && threadIdx.x == 0) *A.any_rebuild = 0;
   for (int u = blockIdx.x; u < cnt; u += gridDim.x) {
     const int4 w = A.units[u];
     const int r = w.x, kind = w.y & 0xFF, mode = w.y >> 8;
@@ -762,6 +764,7 @@ __global__ void __launch_bounds__(kBuildThreads, 1) k_build(DevArrays A, int dyn
         if (threadIdx.x == 0) {
           R->builds += 1;
           R->rebuild = 0;
+          R->near = 0;
         }
         if (R->en_after) replica_energy(A, R, R->cur, red);
       }
@@ -784,10 +787,27 @@ struct ItemCtx {
   int r, off, n, cur, phase, terms, mode, out, ti_dummy;
   long long nl_base, t_cur;
   int L;
-  float a1, a2, a3, a4, amp, T, kbnd, R0sq, fang, half_skin2, pull_f;
+  float a1, a2, a3, a4, amp, T, kbnd, inv_R0sq, fang, half_skin2, pull_f;
   int pull_i, pull_j;
   unsigned seed_lo, seed_hi;
 };
+
+// The step's view of replica r.
+__device__ __forceinline__ ItemCtx load_ctx(const DevArrays& A, int r) {
+  const RepDev* R = &A.rep[r];
+  ItemCtx C;
+  C.r = r; C.off = R->off; C.n = R->n; C.cur = R->cur; C.phase = R->phase;
+  C.terms = R->terms; C.mode = R->mode; C.out = R->out;
+  C.nl_base = R->nl_base; C.t_cur = R->t_cur; C.L = R->L;
+  C.a1 = R->a1; C.a2 = R->a2; C.a3 = R->a3; C.a4 = R->a4;
+  C.amp = R->noise_amp; C.T = R->T; C.kbnd = R->kbnd; C.inv_R0sq = R->inv_R0sq; C.fang = R->fang;
+  C.half_skin2 = R->half_skin2; C.pull_f = R->pull_f; C.pull_i = R->pull_i;
+  C.pull_j = R->pull_j; C.seed_lo = R->seed_lo; C.seed_hi = R->seed_hi;
+  // a list build of this step that failed (row overflow, grid, periodic
+  // image) leaves the replica frozen: no step on incomplete lists
+  if (R->status & (SOP_ST_LIST_OVERFLOW | SOP_ST_PERIODIC | SOP_ST_GRID)) C.phase = PH_SKIP;
+  return C;
+}
 
 template <bool ST>
 __device__ __forceinline__ float4 ldp(const float4* S, int k) {
@@ -801,14 +821,24 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   const long long g = (long long)C.off + i;
   const long long cap = A.cap;
   const float4 hi = ldp<ST>(S, 2 * i), lo = ldp<ST>(S, 2 * i + 1);
-  const int ti = (int)hi.w;
+  const int ti = (int)f2u(hi.w);
   const int4 tp = A.topo[g];
   const int nat_cnt = tp.w & 0xFFFF, bnd_cnt = (tp.w >> 16) & 0xFF, ang_cnt = (tp.w >> 24) & 0xFF;
   const bool upd = (C.phase == PH_FIRST || C.phase == PH_NORMAL) && C.mode != SOP_LIST_NONE;
   const double* Xc = A.X[C.cur];
   const float margin = kScreenMargin;
-  float fx = 0.f, fy = 0.f, fz = 0.f;
+  // every pair / bond / angle contribution is added in int64 fixed point, so
+  // the force is an exact integer sum: independent of list order, of lane
+  // count and of when the lists were built
+  long long Fx = 0, Fy = 0, Fz = 0;
+  float mag = 0.f;  // sum of |contributions| of this lane: bounds the int64 sums, carries NaN/inf
   int st = 0;
+  auto add = [&](float cx, float cy, float cz) {
+    Fx += fixed_from_float(cx);
+    Fy += fixed_from_float(cy);
+    Fz += fixed_from_float(cz);
+    mag += fabsf(cx) + fabsf(cy) + fabsf(cz);
+  };
 
   if (C.terms & SOP_TERM_VDW) {
     // native 12-6 attraction (energy.cpp:274-311).  The force vanishes at the
@@ -823,13 +853,13 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
       const float diff = d2_minus(hi, lo, hj, lj, r0sq, __int_as_float(e.z), dx, dy, dz, d2);
       if (e.x & (int)kPL) {
         if (d2 >= (float)kTol * r0sq) {
-          const int tj = (int)hj.w;
-          const float inv = 1.0f / d2;
+          const int tj = (int)f2u(hj.w);
+          const float inv = __fdividef(1.0f, d2);
           const float u = -diff * inv;                 // s - 1, s = r0^2/d^2
           const float s3m1 = u * fmaf(u, u + 3.0f, 3.0f);  // s^3 - 1
           const float s3 = 1.0f + s3m1;
           const float co = c_ff.fca[ti][tj] * inv * (s3 * s3m1);
-          fx += co * dx; fy += co * dy; fz += co * dz;
+          add(co * dx, co * dy, co * dz);
         }
       }
       if (upd) {
@@ -854,14 +884,14 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
       const float dy = (hj.y - hi.y) + (lj.y - lo.y);
       const float dz = (hj.z - hi.z) + (lj.z - lo.z);
       const float d2 = dx * dx + dy * dy + dz * dz;
-      const int tj = (int)hj.w;
+      const int tj = (int)f2u(hj.w);
       const float s2 = c_ff.s2[ti][tj];
       if (e & (int)kPL) {
         if (d2 >= s2 * (float)kTol) {
-          const float inv = 1.0f / d2;
+          const float inv = __fdividef(1.0f, d2);
           const float s = s2 * inv, s3 = s * s * s;
           const float co = c_ff.fcr[ti][tj] * inv * (2.0f * s3 * s3 + s3);
-          fx += co * dx; fy += co * dy; fz += co * dz;
+          add(co * dx, co * dy, co * dz);
         }
       }
       if (upd) {
@@ -883,11 +913,11 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
       float dx, dy, dz, d2;
       const float diff = d2_minus(hi, lo, hj, lj, r0h, r0l, dx, dy, dz, d2);  // d^2 - r0^2
       const float d = sqrtf(d2);
-      const float dev = diff / (d + r0);
-      const float den = 1.0f - dev * dev / C.R0sq;
+      const float dev = __fdividef(diff, d + r0);
+      const float den = 1.0f - dev * dev * C.inv_R0sq;
       if (!(den > 0.f)) st |= SOP_ST_FENE;
-      const float temp = -C.kbnd * dev / d / den;
-      fx -= temp * dx; fy -= temp * dy; fz -= temp * dz;
+      const float temp = __fdividef(-C.kbnd * dev, d * den);
+      add(-temp * dx, -temp * dy, -temp * dz);
     }
   }
   if (C.terms & SOP_TERM_ANGLE) {
@@ -900,15 +930,13 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
       const float dz = (hj.z - hi.z) + (lj.z - lo.z);
       const float d2 = dx * dx + dy * dy + dz * dz;
       const float d4 = d2 * d2, d8 = d4 * d4;
-      const float co = C.fang / d8;
-      fx -= co * dx; fy -= co * dy; fz -= co * dz;
+      const float co = __fdividef(C.fang, d8);
+      add(-co * dx, -co * dy, -co * dz);
     }
   }
 
-  // lane partials -> int64 fixed point -> exact cross-lane sum
-  long long Fx = fixed_from_float(fx), Fy = fixed_from_float(fy), Fz = fixed_from_float(fz);
-  if (!finite3(fx, fy, fz) || fabsf(fx) > kFixMax || fabsf(fy) > kFixMax || fabsf(fz) > kFixMax)
-    st |= SOP_ST_NONFINITE;
+  // exact cross-lane sum of the fixed-point partials
+  if (!(mag <= kFixMax)) st |= SOP_ST_NONFINITE;  // NaN, inf or out of the fixed-point range
 #pragma unroll
   for (int o = G / 2; o > 0; o >>= 1) {
     Fx += __shfl_xor_sync(gmask, Fx, o, G);
@@ -965,7 +993,13 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
       if (C.mode == SOP_LIST_SKIN) {
         const float4 b = A.xb[g];
         const float ex = h[0] - b.x, ey = h[1] - b.y, ez = h[2] - b.z;
-        if (ex * ex + ey * ey + ez * ez > C.half_skin2) A.rep[C.r].rebuild = 1;
+        const float d2 = ex * ex + ey * ey + ez * ez;
+        if (d2 > C.half_skin2) {
+          A.rep[C.r].rebuild = 1;
+          *A.any_rebuild = 1;
+        } else if (d2 > C.half_skin2 * A.group_frac2) {
+          A.rep[C.r].near = 1;  // may rebuild with the next replica that must
+        }
       }
       if (!(isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]))) st |= SOP_ST_NONFINITE;
     }
@@ -974,8 +1008,9 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   if (st) atomicOr(&A.rep[C.r].status, st);
 }
 
-template <int G>
-__global__ void __launch_bounds__(256, 3) k_step(DevArrays A, const StepItem* items,
+// MB: resident CTAs per SM the register allocation is sized for (2 or 3)
+template <int G, int MB>
+__global__ void __launch_bounds__(256, MB) k_step(DevArrays A, const StepItem* items,
                                                  const int* nitems_dev, int nitems_host) {
   const int nitems = nitems_dev ? *nitems_dev : nitems_host;
   extern __shared__ __align__(128) float4 sst[];
@@ -989,21 +1024,21 @@ __global__ void __launch_bounds__(256, 3) k_step(DevArrays A, const StepItem* it
   fence_async_smem();
   __syncthreads();
   uint32_t parity = 0;
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const StepItem w = items[it];
+  // a contiguous block of items per CTA; consecutive items of one replica
+  // merge into one bead range, staged once, with no barrier inside it
+  const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int it_end = min(nitems, ((int)blockIdx.x + 1) * per);
+  for (int it = (int)blockIdx.x * per; it < it_end;) {
+    StepItem w = items[it];
+    int nx = it + 1;
+    for (; nx < it_end; ++nx) {
+      const StepItem v = items[nx];
+      if (v.r != w.r) break;
+      w.b1 = v.b1;
+    }
+    it = nx;
     if (threadIdx.x == 0) {
-      const RepDev* R = &A.rep[w.r];
-      ItemCtx C;
-      C.r = w.r; C.off = R->off; C.n = R->n; C.cur = R->cur; C.phase = R->phase;
-      C.terms = R->terms; C.mode = R->mode; C.out = R->out;
-      C.nl_base = R->nl_base; C.t_cur = R->t_cur; C.L = R->L;
-      C.a1 = R->a1; C.a2 = R->a2; C.a3 = R->a3; C.a4 = R->a4;
-      C.amp = R->noise_amp; C.T = R->T; C.kbnd = R->kbnd; C.R0sq = R->R0sq; C.fang = R->fang;
-      C.half_skin2 = R->half_skin2; C.pull_f = R->pull_f; C.pull_i = R->pull_i;
-      C.pull_j = R->pull_j; C.seed_lo = R->seed_lo; C.seed_hi = R->seed_hi;
-      // a list build of this step that failed (row overflow, grid, periodic
-      // image) leaves the replica frozen: no step on incomplete lists
-      if (R->status & (SOP_ST_LIST_OVERFLOW | SOP_ST_PERIODIC | SOP_ST_GRID)) C.phase = PH_SKIP;
+      const ItemCtx C = load_ctx(A, w.r);
       sC = C;
       if (C.phase != PH_SKIP && w.staged) {
         const char* src = reinterpret_cast<const char*>(A.stage[C.cur] + 2 * (long long)C.off);
@@ -1038,6 +1073,40 @@ __global__ void __launch_bounds__(256, 3) k_step(DevArrays A, const StepItem* it
   }
 }
 
+// The same step with warps as independent workers: each warp takes work items
+// from a global counter and steps their beads 32/G at a time, gathering
+// partner positions through L1/L2 (no shared-memory staging, no block
+// barriers, dynamic balance).  Per-bead arithmetic is step_bead's, so results
+// are bit-identical to k_step's.  ctr[0] hands out items, ctr[1] counts
+// finished warps; the last warp resets both for the next launch.
+template <int G, int MB>
+__global__ void __launch_bounds__(256, MB) k_step_w(DevArrays A, const StepItem* items,
+                                                   const int* nitems_dev, int nitems_host) {
+  const int nitems = nitems_dev ? *nitems_dev : nitems_host;
+  const int l32 = threadIdx.x & 31;
+  const int lane = l32 & (G - 1), grp = l32 / G;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (l32 & ~(G - 1)));
+  for (;;) {
+    int it = 0;
+    if (l32 == 0) it = atomicAdd(A.step_ctr, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= nitems) break;
+    const StepItem w = items[it];
+    const ItemCtx C = load_ctx(A, w.r);
+    if (C.phase == PH_SKIP) continue;
+    const float4* S = A.stage[C.cur] + 2 * (long long)C.off;
+    for (int b = w.b0 + grp; b < w.b1; b += 32 / G) step_bead<G, false>(A, C, S, b, lane, gmask);
+  }
+  if (l32 == 0) {
+    __threadfence();
+    const int warps = (int)(gridDim.x * (blockDim.x >> 5));
+    if (atomicAdd(A.step_ctr + 1, 1) == warps - 1) {
+      A.step_ctr[0] = 0;
+      A.step_ctr[1] = 0;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------
 // K5: energies in FP64 (energy.cpp:115-257), deterministic fixed-order sums
 
@@ -1061,12 +1130,13 @@ __device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* r
   const long long cap = A.cap;
   const double* X = A.X[buf];
   const float4* S = A.stage[buf];
-  double eb = 0, ea = 0, eatt = 0, erep = 0;
+  double eb = 0, ea = 0, eatt = 0;
+  long long erep_fx = 0;  // list-ordered sum: exact in fixed point (2^-40 kcal/mol)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const long long gi = off + i;
     const int4 tp = A.topo[gi];
     const int nat_cnt = tp.w & 0xFFFF, bnd_cnt = (tp.w >> 16) & 0xFF, ang_cnt = (tp.w >> 24) & 0xFF;
-    const int ti = (int)S[2 * gi].w;
+    const int ti = (int)f2u(S[2 * gi].w);
     if (R->terms & SOP_TERM_FENE)
       for (int k = 0; k < bnd_cnt; k++) {
         const int j = A.bnd[tp.y + k].x;
@@ -1087,7 +1157,7 @@ __device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* r
         const int4 e = A.nat[tp.x + k];
         const int j = e.x & (int)kIdx;
         if (j <= i || !(e.x & (int)kPL)) continue;
-        const int tj = (int)S[2 * (off + (long long)j)].w;
+        const int tj = (int)f2u(S[2 * (off + (long long)j)].w);
         const double r0 = A.nat_r0[tp.x + k];
         const double r2 = r0 * r0, r6 = r2 * r2 * r2, r12 = r6 * r6;
         const double d2 = exact_d2(X, cap, gi, off + j);
@@ -1100,14 +1170,15 @@ __device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* r
         const int e = A.nl[row + k];
         const int j = e & (int)kIdx;
         if (j <= i || !(e & (int)kPL)) continue;
-        const int tj = (int)S[2 * (off + (long long)j)].w;
+        const int tj = (int)f2u(S[2 * (off + (long long)j)].w);
         const double d2 = exact_d2(X, cap, gi, off + j);
         const double d6 = d2 * d2 * d2, d12 = d6 * d6;
-        erep += c_ff.coeff_rep[ti][tj] * (c_ff.sigma_rep12[ti][tj] / d12 + c_ff.sigma_rep6[ti][tj] / d6);
+        const double ep = c_ff.coeff_rep[ti][tj] * (c_ff.sigma_rep12[ti][tj] / d12 + c_ff.sigma_rep6[ti][tj] / d6);
+        erep_fx += __double2ll_rn(ep * 1099511627776.0);  // 2^40
       }
     }
   }
-  double v[4] = {eb, ea, eatt, erep};
+  double v[4] = {eb, ea, eatt, (double)erep_fx * 9.094947017729282e-13};  // 2^-40
   block_sum(v, 4, red);
   if (threadIdx.x == 0) {
     R->energy[0] = -R->e_bnd_coeff * v[0];
@@ -1184,7 +1255,7 @@ __global__ void k_pairlist(DevArrays A, int r, int off, int n) {
   const double* X = A.X[R->cur];
   const float4* S = A.stage[R->cur] + 2 * (long long)off;
   const float4 hi = S[2 * i], lo = S[2 * i + 1];
-  const int ti = (int)hi.w;
+  const int ti = (int)f2u(hi.w);
   const int4 tp = A.topo[gi];
   const int nat_cnt = tp.w & 0xFFFF;
   for (int k = 0; k < nat_cnt; k++) {
@@ -1210,7 +1281,7 @@ __global__ void k_pairlist(DevArrays A, int r, int off, int n) {
     const float dx = (hj.x - hi.x) + (lj.x - lo.x), dy = (hj.y - hi.y) + (lj.y - lo.y),
                 dz = (hj.z - hi.z) + (lj.z - lo.z);
     const float d2 = dx * dx + dy * dy + dz * dz;
-    const int tj = (int)hj.w;
+    const int tj = (int)f2u(hj.w);
     const double rc2 = c_ff.rc2_pl[ti][tj];
     const bool plb = within(d2, c_ff.rc2_pl_f[ti][tj], kScreenMargin,
                             [&] { return exact_d2(X, cap, gi, off + j) < rc2; });
@@ -1306,10 +1377,31 @@ __global__ void k_export(DevArrays A, int r, int off, int n, int which, int capa
 // ---------------------------------------------------------------------------------
 // launchers
 
-static int g_build_dyn = 48 * 1024;  // k_build dynamic shared memory (set by init_kernels)
-static int g_bin_dyn = 48 * 1024;    // k_bin dynamic shared memory
+using StepKernel = void (*)(DevArrays, const StepItem*, const int*, int);
 
-// Opt every kernel into the device's full per-block shared memory once.
+// The step kernel for a strategy (0: CTA items with shared-memory staging,
+// 1: warp tasks), lane count (1, 2, 4, 8, 16) and occupancy target (2, 3).
+template <int G>
+static StepKernel step_kernel_g(int strategy, int min_blocks) {
+  const bool two = min_blocks == 2;
+  if (strategy == 1) return two ? k_step_w<G, 2> : k_step_w<G, 3>;
+  return two ? k_step<G, 2> : k_step<G, 3>;
+}
+static StepKernel step_kernel(int lanes, int min_blocks, int strategy) {
+  switch (lanes) {
+    case 1: return step_kernel_g<1>(strategy, min_blocks);
+    case 2: return step_kernel_g<2>(strategy, min_blocks);
+    case 8: return step_kernel_g<8>(strategy, min_blocks);
+    case 16: return step_kernel_g<16>(strategy, min_blocks);
+    default: return step_kernel_g<4>(strategy, min_blocks);
+  }
+}
+
+static int g_build_dyn = 48 * 1024;  // k_build dynamic shared memory (set by init_kernels)
+static int g_bin_dyn = 48 * 1024;    // k_prologue dynamic shared memory
+
+// Opt a kernel into up to `optin_bytes` of dynamic shared memory per block
+// (less its static shared memory and the per-block reservation).
 template <class K>
 static cudaError_t optin(K kernel, int optin_bytes, int* dyn_out = nullptr) {
   cudaFuncAttributes fa;
@@ -1320,15 +1412,15 @@ static cudaError_t optin(K kernel, int optin_bytes, int* dyn_out = nullptr) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
 }
 
-cudaError_t init_kernels(int optin_bytes) {
+cudaError_t init_kernels(int optin_bytes, int sm_bytes) {
   cudaError_t e;
-  if ((e = optin(k_build, optin_bytes, &g_build_dyn)) != cudaSuccess) return e;
-  if ((e = optin(k_bin, optin_bytes, &g_bin_dyn)) != cudaSuccess) return e;
-  if ((e = optin(k_step<1>, optin_bytes)) != cudaSuccess) return e;
-  if ((e = optin(k_step<2>, optin_bytes)) != cudaSuccess) return e;
-  if ((e = optin(k_step<4>, optin_bytes)) != cudaSuccess) return e;
-  if ((e = optin(k_step<8>, optin_bytes)) != cudaSuccess) return e;
-  if ((e = optin(k_step<16>, optin_bytes)) != cudaSuccess) return e;
+  // the prologue kernels run two CTAs per SM: half the SM's shared memory each
+  const int half = std::min(optin_bytes, sm_bytes / 2);
+  if ((e = optin(k_build, half, &g_build_dyn)) != cudaSuccess) return e;
+  if ((e = optin(k_prologue, half, &g_bin_dyn)) != cudaSuccess) return e;
+  for (int lanes : {1, 2, 4, 8, 16})
+    for (int mb : {2, 3})
+      if ((e = optin(step_kernel(lanes, mb, 0), optin_bytes)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 
@@ -1336,13 +1428,11 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, co
                             int force_build, int build_mode, int grid, cudaStream_t s,
                             cudaEvent_t after_decide, cudaEvent_t after_bin) {
   if (nrep <= 0) return cudaSuccess;
-  const int dgrid = (nrep + 127) / 128;
-  k_decide<<<dgrid, 128, 0, s>>>(A, rep_ids, nrep_dev, nrep, force_build, build_mode);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  cudaError_t e;
   if (after_decide && (e = cudaEventRecord(after_decide, s)) != cudaSuccess) return e;
   if (grid <= 0) grid = 1;
-  k_bin<<<grid, kBinThreads, g_bin_dyn, s>>>(A, g_bin_dyn);
+  k_prologue<<<grid, kBinThreads, g_bin_dyn, s>>>(A, rep_ids, nrep_dev, nrep, force_build, build_mode,
+                                                  g_bin_dyn);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (after_bin && (e = cudaEventRecord(after_bin, s)) != cudaSuccess) return e;
   // the energy / observables units use the same memory as a reduction buffer
@@ -1351,42 +1441,23 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, co
   return cudaGetLastError();
 }
 
-template <int G>
-static cudaError_t launch_step_g(const DevArrays& A, const StepItem* items, int nitems,
-                                 const int* nitems_dev, size_t dyn, int threads, int grid,
-                                 cudaStream_t s) {
-  k_step<G><<<grid, threads, dyn, s>>>(A, items, nitems_dev, nitems);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
-                        int max_staged, int lanes, int threads, int grid, cudaStream_t s) {
+                        int max_staged, int lanes, int min_blocks, int strategy, int threads,
+                        int grid, cudaStream_t s) {
   if (nitems <= 0) return cudaSuccess;
-  size_t dyn = (size_t)max_staged * 32 + 128;
+  const size_t dyn = strategy == 1 ? 0 : (size_t)max_staged * 32 + 128;
   if (grid <= 0) grid = nitems;
-  switch (lanes) {
-    case 1: return launch_step_g<1>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
-    case 2: return launch_step_g<2>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
-    case 8: return launch_step_g<8>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
-    case 16: return launch_step_g<16>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
-    default: return launch_step_g<4>(A, items, nitems, nitems_dev, dyn, threads, grid, s);
-  }
+  step_kernel(lanes, min_blocks, strategy)<<<grid, threads, dyn, s>>>(A, items, nitems_dev, nitems);
+  return cudaGetLastError();
 }
 
 int step_kernel_max_smem() { return kStageMax * 32 + 128; }
 
-int step_blocks_per_sm(int lanes, int threads, int max_staged) {
-  const size_t dyn = (size_t)max_staged * 32 + 128;
+int step_blocks_per_sm(int lanes, int min_blocks, int strategy, int threads, int max_staged) {
+  const size_t dyn = strategy == 1 ? 0 : (size_t)max_staged * 32 + 128;
   int n = 0;
-  cudaError_t e;
-  switch (lanes) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<1>, threads, dyn); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<2>, threads, dyn); break;
-    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<8>, threads, dyn); break;
-    case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<16>, threads, dyn); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<4>, threads, dyn); break;
-  }
-  if (e != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel(lanes, min_blocks, strategy),
+                                                    threads, dyn) != cudaSuccess) {
     cudaGetLastError();
     return 1;
   }

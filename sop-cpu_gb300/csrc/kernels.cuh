@@ -45,11 +45,10 @@ struct DevArrays {
   int* cstart;        // per replica cell range (RepDev::cell_base): exclusive prefix of cell counts
   int* ccur;          // same layout: scatter cursors
   struct BinHdr* bin_hdr;  // per replica: grid of the last binning
-  int4* bins;         // binning queue {replica, mode, buffer, 0}
-  int* bin_cnt;
-  int* bin_exit;
-  int bin_cap;
   int slice_beads;    // beads per list-build slice unit
+  int* step_ctr;      // warp-task step kernel: {next item, finished warps}
+  int* any_rebuild;   // a SKIN displacement trigger fired in the last step
+  float group_frac2;  // (grouping fraction of the trigger distance)^2; > 1 = no grouping
 };
 
 // Grid of one replica's last binning.
@@ -72,28 +71,35 @@ struct StepItem {
 constexpr int kStageMax = 6144;       // beads staged in shared memory (192 KB)
 constexpr int kBuildThreads = 512;
 constexpr int kBinThreads = 512;
-// kernel launches of one step: k_decide, k_bin, k_build (prologue), k_step
-constexpr int kPrologueLaunches = 3;
-constexpr int kStepLaunches = 4;
+// kernel launches of one step: k_prologue (bookkeeping + binning), k_build, k_step
+constexpr int kPrologueLaunches = 2;
+constexpr int kStepLaunches = 3;
 // cells a replica's binning may use (grid cells grow wider beyond that)
 inline long long cell_capacity(int n) { return 4LL * n + 4096; }
 
 void upload_tables(const FFTables& t, cudaStream_t s);
-// Opt the kernels into `optin_bytes` of shared memory per block (once per device).
-cudaError_t init_kernels(int optin_bytes);
+// Opt the kernels into shared memory (once per device): optin_bytes per block
+// at most, sm_bytes per SM.
+cudaError_t init_kernels(int optin_bytes, int sm_bytes);
 
-// Prologue + list build over `nrep` replica ids: k_decide, k_bin (one CTA per
-// replica to bin), k_build (persistent CTAs over slices, energies, observables).
+// Prologue + list build over `nrep` replica ids: k_prologue (bookkeeping, and
+// cell binning of the replicas that rebuild), k_build (persistent CTAs over
+// list slices, energies, observables).
 // force_build: build for every listed replica from the CURRENT buffer
 // (reference-named list updates), else the step cadence decides.
 // nrep / nitems: host counts (grid sizing); *_dev: the same counts in device
 // memory, read by the kernels when given (graphs survive layout changes).
-// after_decide / after_bin: events recorded between the three kernels (profiling)
+// after_decide / after_bin: events recorded before and after k_prologue (profiling)
 cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, const int* nrep_dev,
                             int force_build, int build_mode, int grid, cudaStream_t s,
                             cudaEvent_t after_decide = nullptr, cudaEvent_t after_bin = nullptr);
+// min_blocks: the step-kernel variant whose registers are sized for 2 or 3
+// resident CTAs per SM
+// strategy: 0 = CTA work items with shared-memory staging (k_step), 1 = warp
+// tasks gathering through L1/L2 (k_step_w); bit-identical results
 cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
-                        int max_staged, int lanes, int threads, int grid, cudaStream_t s);
+                        int max_staged, int lanes, int min_blocks, int strategy, int threads,
+                        int grid, cudaStream_t s);
 cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s);
 cudaError_t launch_observables(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s);
 cudaError_t launch_pairlist(const DevArrays& A, int r, int off, int n, cudaStream_t s);
@@ -106,6 +112,6 @@ cudaError_t launch_export(const DevArrays& A, int r, int off, int n, int which, 
                           cudaStream_t s);
 int step_kernel_max_smem();
 // resident step-kernel CTAs per SM for this configuration
-int step_blocks_per_sm(int lanes, int threads, int max_staged);
+int step_blocks_per_sm(int lanes, int min_blocks, int strategy, int threads, int max_staged);
 
 }  // namespace sop

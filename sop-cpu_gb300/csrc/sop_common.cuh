@@ -61,7 +61,7 @@ struct RepDev {
   double a1d, a2d, a3d, a4d;
   float noise_amp;         // sqrt(2 T zeta / h)
   float T;
-  float kbnd, R0sq;        // FENE
+  float kbnd, R0sq, inv_R0sq;  // FENE
   float fang;              // 6 eps sigma_ss^6 (soft-sphere force coefficient)
   double kbnd_d, R0sq_d, fang_d, e_bnd_coeff, e_ang_coeff;
   float pull_f;            // pulling force magnitude, kcal/mol/A
@@ -77,6 +77,7 @@ struct RepDev {
   int cur;                 // position buffer holding X_t for this step
   int inlup;               // reference cadence counter (sop.cpp:100,156-165)
   int rebuild;             // rebuild requested (SKIN displacement or host)
+  int near;                // SKIN displacement past the grouping fraction of the trigger
   int out;                 // this step is an output step
   int obs_pending;         // observables of the last output step still due
   int en_after;            // energies due after this step's list build
@@ -226,7 +227,8 @@ SOP_HD float d2f_exact(double d) {
 // kcal/mol/A, range +-1.3e8 over 16 lanes) through two F2I.S32 conversions,
 // so the cross-lane reduction is exact and order-free.  With t = f * 2^36,
 // a = rint(t / 2^32) and r = t - a * 2^32 is exact (Sterbenz), |r| <= 2^31.
-// |f| must stay below kFixMax; larger lane sums are flagged by the caller.
+// |f| must stay below kFixMax; a lane whose sum of |contributions| exceeds it
+// is flagged by the caller (so that int64 sums over up to 16 lanes cannot wrap).
 constexpr float kFixMax = 4.0e6f;
 SOP_HD long long fixed_from_float(float f) {
   const float t = f * 68719476736.0f;  // 2^36

@@ -74,6 +74,7 @@ class EngineConfig(C.Structure):
         ("max_list_entries", C.c_int64), ("block_threads", C.c_int),
         ("lanes_per_bead", C.c_int), ("graph_steps", C.c_int),
         ("stage_limit", C.c_int), ("chunk_beads", C.c_int), ("build_slice_beads", C.c_int),
+        ("step_min_blocks", C.c_int), ("step_strategy", C.c_int), ("group_rebuild_pct", C.c_int),
     ]
 
 

@@ -61,14 +61,20 @@ def main(argv=None):
     ap.add_argument("case", choices=("mix", "build", "globule"))
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warm", type=int, default=10, help="batched steps before the profiled ones")
+    ap.add_argument("--tune", type=int, default=0,
+                    help="autotune with this many steps per trial before profiling")
     a = ap.parse_args(argv)
     eng, systems = {"mix": mix_engine, "build": build_engine, "globule": globule_engine}[a.case]()
     if a.warm:
         eng.run(a.warm)
+    if a.tune:
+        t = eng.profile_split(a.steps)
+        print("untuned: " + " ".join("%s_ms=%.4f" % kv for kv in t.items()))
+        print(eng.autotune(a.tune), end="")
     t = eng.profile_split(a.steps)
-    print("case=%s replicas=%d beads=%d decide_ms=%.4f bin_ms=%.4f build_ms=%.4f step_ms=%.4f"
-          % (a.case, len(systems), sum(s.nbead for s in systems), t["decide"], t["bin"],
-             t["build"], t["step"]))
+    print("case=%s replicas=%d beads=%d prologue_ms=%.4f build_ms=%.4f step_ms=%.4f"
+          % (a.case, len(systems), sum(s.nbead for s in systems), t["prologue"], t["build"],
+             t["step"]))
     eng.close()
     return 0
 

@@ -223,10 +223,11 @@ class Engine:
         return s.value, p.value
 
     def profile_split(self, nsteps: int):
-        """Mean ms per step of k_decide, k_bin, k_build and k_step (CUDA events)."""
+        """Mean ms per step of k_prologue (bookkeeping + binning), k_build and
+        k_step (CUDA events)."""
         out = (C.c_double * 4)()
         L.check(L.lib().sop_profile_steps_ex(self.h, int(nsteps), out), "sop_profile_steps_ex")
-        return dict(zip(("decide", "bin", "build", "step"), list(out)))
+        return {"prologue": out[0] + out[1], "build": out[2], "step": out[3]}
 
     def launches(self) -> int:
         n = C.c_int64()

@@ -1,10 +1,9 @@
 """Autotuner (sop_autotune_ex).  Its trials are real steps of one run window:
-launch-shape tuning must leave every trajectory bit-identical to a plain
-sop_run of the same step count, and skin / cell-edge tuning must keep the
-pair list feeding each step equal to the reference's (3.2x / nnlup) pair
-sets.  Tolerances: bit-identical state for shape tuning; pair sets exact and
-positions within 1e-6 A RMSD for list tuning (row order only moves float
-rounding)."""
+tuning must leave every trajectory bit-identical to a plain sop_run of the
+same step count, and skin / cell-edge tuning must keep the pair list feeding
+each step equal to the reference's (3.2x / nnlup) pair sets.  Forces are
+exact fixed-point sums of their contributions, so the tolerance is bit
+identity throughout."""
 import re
 
 import numpy as np
@@ -74,7 +73,28 @@ def test_list_tuning_keeps_reference_pair_sets():
         for _ in range(2):
             for k in (2, 3):
                 np.testing.assert_array_equal(pairset(*e.pairs(a, k)), pairset(*e.pairs(b, k)))
-            xa, xb = e.state(a)[1], e.state(b)[1]
-            assert float(np.sqrt(((xa - xb) ** 2).sum(1).mean())) < 1e-6
+            np.testing.assert_array_equal(e.state(a)[1], e.state(b)[1])
             assert e.status(a)[0] == 0 and e.status(b)[0] == 0
             e.run(150)  # and the tuned list keeps tracking after the tuner
+
+
+@pytest.mark.parametrize("cfg", [dict(step_strategy=1), dict(step_strategy=1, step_min_blocks=2),
+                                 dict(stage_limit=-1), dict(build_slice_beads=128, chunk_beads=64),
+                                 dict(lanes_per_bead=4), dict(lanes_per_bead=1),
+                                 dict(group_rebuild_pct=-1), dict(group_rebuild_pct=90)])
+def test_launch_shapes_bit_identical(cfg):
+    """Every launch shape, both step strategies (CTA items staged in shared
+    memory, warp tasks through L1/L2), every lane count and rebuild grouping
+    give the same trajectories: each force is an exact integer sum of its
+    pair contributions, whatever the list order or the build times."""
+    systems = [S.synth_chain(8400 + k, n) for k, n in enumerate([60, 700, 2600, 5000, 130])]
+    params = [make_params(script(), seed=4400 + k, list_mode="skin" if k % 2 else "neighborlist",
+                          skin=2.0) for k in range(len(systems))]
+    out = []
+    for c in ({}, cfg):
+        with Engine(0, max_beads=1 << 15, max_replicas=16, max_list_entries=1 << 23, **c) as e:
+            ids = [e.add(s, p) for s, p in zip(systems, params)]
+            e.run(250)
+            out.append([e.state(r)[1] for r in ids])
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
