@@ -61,6 +61,10 @@ extern "C" {
 #define SOP_TERM_VDW 0x8
 #define SOP_TERM_ALL 0xF
 
+/* integrators (set dynamics, params.cpp:19-31) */
+#define SOP_DYN_UNDERDAMPED 0 /* underdamped_iteration, sop.cpp:282-329 */
+#define SOP_DYN_OVERDAMPED 1  /* overdamped_iteration, sop.cpp:331-363  */
+
 /* integrator precision */
 #define SOP_PREC_MIXED 0 /* FP32 pair forces, FP64 positions (default)      */
 #define SOP_PREC_FP64 1  /* FP64 pair forces and update (drift reference)   */
@@ -88,6 +92,8 @@ typedef struct sop_params {
   int force_terms; /* SOP_TERM_* mask                                       */
   int precision;  /* SOP_PREC_*                                             */
   int pull_i, pull_j; /* pulled beads (default first and last)              */
+  int dynamics;   /* SOP_DYN_UNDERDAMPED (sim_type 1) or SOP_DYN_OVERDAMPED (2) */
+  double a5;      /* overdamped step factor h/zeta (params.cpp:31, 91, 392)  */
 } sop_params;
 
 /* One system: topology + initial state.  All arrays 0-based, borrowed. */
@@ -115,8 +121,7 @@ typedef struct sop_engine_config {
   int max_replicas;      /* replica slots (0 = 4096)                           */
   int64_t max_list_entries; /* neighbor-list entry capacity (0 = 64 per bead)  */
   int block_threads;     /* fused step kernel block size, 64..256 (0 = 256)   */
-  int lanes_per_bead;    /* lanes cooperating on one bead: 1,2,4,8,16 (0 = 2); the
-                            only knob that changes float summation order      */
+  int lanes_per_bead;    /* lanes cooperating on one bead: 1,2,4,8,16 (0 = 2)  */
   int graph_steps;       /* steps captured per CUDA graph launch (0 = 20)      */
   int stage_limit;       /* largest replica (beads) whose positions the step
                             kernel stages in shared memory by TMA; larger ones
@@ -213,6 +218,18 @@ int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_kernel_ms, dou
  * the prologue (~0), ms[1] k_prologue (bookkeeping + cell binning), ms[2]
  * k_build (list slices, energies, observables), ms[3] k_step. */
 int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms);
+
+/* ---- checkpoint / restart ------------------------------------------------------ */
+/* Exact snapshot of one replica (both position buffers, increments,
+ * velocities, list rows with their pair-list bits, native flags, skin
+ * references, step / noise counters and cadence), in place of the reference's
+ * restart files (sop.cpp:132-140: coordinates, velocities, generator state).
+ * buf == NULL: *size receives the bytes needed.  SOP_ERR_OVERFLOW if cap is
+ * too small.  Restoring into a replica of the same system (any engine, any
+ * launch configuration) continues the run bit for bit; the target keeps its
+ * own parameters.  Call between runs or run chunks. */
+int sop_replica_checkpoint(sop_engine* e, int replica, void* buf, int64_t cap, int64_t* size);
+int sop_replica_restore(sop_engine* e, int replica, const void* buf, int64_t size);
 
 /* ---- autotuner --------------------------------------------------------------- */
 /* No reference counterpart.  Time the batched step of the active replicas

@@ -80,9 +80,13 @@ void sopref_pair_list() { update_pair_list(); }
 void sopref_force_eval() { force_eval(); }
 void sopref_energy_eval() { energy_eval(); }
 void sopref_observables() { calculate_observables(h_incr); }
-void sopref_iteration() { underdamped_iteration(h_incr); }
+void sopref_iteration() {
+  if (sim_type == 2) overdamped_iteration(h_incr);
+  else underdamped_iteration(h_incr);
+}
 
-// n iterations of the underdamped_ctrl loop body (sop.cpp:153-172).
+// n iterations of the underdamped_ctrl loop body (sop.cpp:153-172); the
+// overdamped_ctrl body (sop.cpp:425-444) has the same schedule.
 void sopref_run(int nsteps) {
   for (int s = 0; s < nsteps; s++) {
     if ((h_inlup % nnlup) == 0) {
@@ -92,7 +96,8 @@ void sopref_run(int nsteps) {
     }
     h_inlup++;
     if (neighborlist == 1 || celllist == 1) update_pair_list();
-    underdamped_iteration(h_incr);
+    if (sim_type == 2) overdamped_iteration(h_incr);
+    else underdamped_iteration(h_incr);
   }
 }
 

@@ -1009,9 +1009,17 @@ void sopo_observables(sopo_sys* s) {
   rg /= (double)(s->nbead * s->nbead);
   s->rgsq = rg;
   double sv = 0.0;
-  for (int i = 0; i < s->nbead; i++) {
-    const double* v = s->vel + 3 * i;
-    sv += v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  if (s->sim_type == 2) {  /* overdamped: from the last increments (sop.cpp:270-278) */
+    for (int i = 0; i < s->nbead; i++) {
+      const double* v = s->incr + 3 * i;
+      sv += v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    }
+    sv *= s->zeta / (2.0 * s->h);
+  } else {
+    for (int i = 0; i < s->nbead; i++) {
+      const double* v = s->vel + 3 * i;
+      sv += v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    }
   }
   s->kinT = sv / (3.0 * (double)s->nbead);
 }
@@ -1022,6 +1030,16 @@ void sopo_observables(sopo_sys* s) {
 void sopo_iteration(sopo_sys* s) {
   const double eps = 1.0e-5;
   double *pos = s->pos, *unc = s->unc_pos, *vel = s->vel, *f = s->force, *inc = s->incr;
+  if (s->sim_type == 2) {  /* overdamped_iteration (sop.cpp:331-363) */
+    for (int q = 0; q < 3 * s->nbead; q++) {
+      inc[q] = s->a5 * f[q];
+      unc[q] += inc[q];
+      pos[q] += inc[q];
+      pos[q] -= s->boxl * rnd(pos[q] / s->boxl);
+    }
+    sopo_force_eval(s);
+    return;
+  }
   for (int q = 0; q < 3 * s->nbead; q++) {
     inc[q] = s->a1 * vel[q] + s->a2 * f[q];
     pos[q] += inc[q];

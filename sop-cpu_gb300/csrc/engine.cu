@@ -176,6 +176,8 @@ extern "C" void sop_params_default(sop_params* p) {
   p->precision = SOP_PREC_MIXED;
   p->pull_i = 0;
   p->pull_j = -1;
+  p->dynamics = SOP_DYN_UNDERDAMPED;
+  p->a5 = p->h / p->zeta;  // params.cpp:392
 }
 
 extern "C" void sop_engine_config_default(sop_engine_config* c) {
@@ -403,9 +405,14 @@ static int fill_repdev(const sop_params& p, RepDev& d) {
   d.fang = (float)d.fang_d;
   d.e_bnd_coeff = p.k_bnd * (p.R0 * p.R0) / 2.0;
   d.pull_f = (float)p.pull_force;
+  d.dyn = p.dynamics;
+  d.a5 = (float)p.a5;
+  d.a5d = p.a5;
+  d.zeta_2h = (p.h > 0) ? p.zeta / (2.0 * p.h) : 0.0;
   d.seed_lo = (uint32_t)p.seed;
   d.seed_hi = (uint32_t)(p.seed >> 32);
   if (p.list_mode < SOP_LIST_NONE || p.list_mode > SOP_LIST_SKIN) return SOP_ERR_ARG;
+  if (p.dynamics != SOP_DYN_UNDERDAMPED && p.dynamics != SOP_DYN_OVERDAMPED) return SOP_ERR_ARG;
   if (p.precision != SOP_PREC_MIXED) return SOP_ERR_UNSUPPORTED;
   return SOP_OK;
 }
@@ -894,6 +901,7 @@ extern "C" int sop_replica_set_params(sop_engine* e, int r, const sop_params* p)
   d.inv_R0sq = cfg.inv_R0sq;
   d.kbnd_d = cfg.kbnd_d; d.R0sq_d = cfg.R0sq_d; d.fang = cfg.fang; d.fang_d = cfg.fang_d;
   d.e_bnd_coeff = cfg.e_bnd_coeff; d.e_ang_coeff = cfg.e_ang_coeff; d.pull_f = cfg.pull_f;
+  d.dyn = cfg.dyn; d.a5 = cfg.a5; d.a5d = cfg.a5d; d.zeta_2h = cfg.zeta_2h;
   d.seed_lo = cfg.seed_lo; d.seed_hi = cfg.seed_hi;
   int pi = p->pull_i, pj = p->pull_j;
   d.pull_i = (pi >= 0 && pi < R.n) ? pi : 0;

@@ -787,7 +787,8 @@ struct ItemCtx {
   int r, off, n, cur, phase, terms, mode, out, ti_dummy;
   long long nl_base, t_cur;
   int L;
-  float a1, a2, a3, a4, amp, T, kbnd, inv_R0sq, fang, half_skin2, pull_f;
+  float a1, a2, a3, a4, a5, amp, T, kbnd, inv_R0sq, fang, half_skin2, pull_f;
+  int dyn;
   int pull_i, pull_j;
   unsigned seed_lo, seed_hi;
 };
@@ -799,7 +800,7 @@ __device__ __forceinline__ ItemCtx load_ctx(const DevArrays& A, int r) {
   C.r = r; C.off = R->off; C.n = R->n; C.cur = R->cur; C.phase = R->phase;
   C.terms = R->terms; C.mode = R->mode; C.out = R->out;
   C.nl_base = R->nl_base; C.t_cur = R->t_cur; C.L = R->L;
-  C.a1 = R->a1; C.a2 = R->a2; C.a3 = R->a3; C.a4 = R->a4;
+  C.a1 = R->a1; C.a2 = R->a2; C.a3 = R->a3; C.a4 = R->a4; C.a5 = R->a5; C.dyn = R->dyn;
   C.amp = R->noise_amp; C.T = R->T; C.kbnd = R->kbnd; C.inv_R0sq = R->inv_R0sq; C.fang = R->fang;
   C.half_skin2 = R->half_skin2; C.pull_f = R->pull_f; C.pull_i = R->pull_i;
   C.pull_j = R->pull_j; C.seed_lo = R->seed_lo; C.seed_hi = R->seed_hi;
@@ -964,25 +965,36 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
     for (int c = 0; c < 3; c++) A.force[c * cap + g] = f2d_exact(F[c]);
   }
   if (C.phase != PH_FORCE) {
-    const bool keepv = (C.phase == PH_FIRST) || (C.T < (float)kEpsT);
-    float v[3];
-    for (int c = 0; c < 3; c++) {
-      if (keepv) {
-        float h, l;
-        split_double(A.vel[c * cap + g], h, l);
-        v[c] = h;
-      } else {
-        v[c] = C.a3 * A.incr[c * cap + g] + C.a4 * F[c];
+    float inc3[3];
+    if (C.dyn == SOP_DYN_OVERDAMPED) {
+      // overdamped_iteration (sop.cpp:331-363): incr = a5 F, no velocities; at
+      // output steps the velocity array keeps the finished iteration's
+      // increment, which calculate_observables reads (sop.cpp:270-278)
+      if (C.phase != PH_FIRST && (C.out || C.phase == PH_FINAL))
+        for (int c = 0; c < 3; c++) A.vel[c * cap + g] = f2d_exact(A.incr[c * cap + g]);
+      for (int c = 0; c < 3; c++) inc3[c] = C.a5 * F[c];
+    } else {
+      const bool keepv = (C.phase == PH_FIRST) || (C.T < (float)kEpsT);
+      float v[3];
+      for (int c = 0; c < 3; c++) {
+        if (keepv) {
+          float h, l;
+          split_double(A.vel[c * cap + g], h, l);
+          v[c] = h;
+        } else {
+          v[c] = C.a3 * A.incr[c * cap + g] + C.a4 * F[c];
+        }
       }
+      if (!keepv && (C.out || C.phase == PH_FINAL))
+        for (int c = 0; c < 3; c++) A.vel[c * cap + g] = f2d_exact(v[c]);
+      for (int c = 0; c < 3; c++) inc3[c] = C.a1 * v[c] + C.a2 * F[c];
     }
-    if (!keepv && (C.out || C.phase == PH_FINAL))
-      for (int c = 0; c < 3; c++) A.vel[c * cap + g] = f2d_exact(v[c]);
     if (C.phase != PH_FINAL) {
       const int nb = C.cur ^ 1;
       float h[3], l[3];
       double xn[3];
       for (int c = 0; c < 3; c++) {
-        const float inc = C.a1 * v[c] + C.a2 * F[c];
+        const float inc = inc3[c];
         xn[c] = Xc[c * cap + g] + f2d_exact(inc);  // the FP64 accumulation
         A.X[nb][c * cap + g] = xn[c];
         A.incr[c * cap + g] = inc;
@@ -1225,7 +1237,8 @@ __device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red)
     R->obs[1] = q[0];
     R->obs[0] = q[1] > 0 ? q[0] / q[1] : 0.0;
     R->obs[2] = q[2] / n;  // sum_{i<j} d^2 / N^2 = sum |r - mean|^2 / N
-    R->obs[3] = q[3] / (3.0 * n);
+    // kinT (sop.cpp:262-279): overdamped from the last increments, kept in vel
+    R->obs[3] = (R->dyn == SOP_DYN_OVERDAMPED ? q[3] * R->zeta_2h : q[3]) / (3.0 * n);
     R->obs[4] = sqrt(exact_d2(X, cap, (long long)off, (long long)off + n - 1));
   }
 }

@@ -65,6 +65,9 @@ struct RepDev {
   float fang;              // 6 eps sigma_ss^6 (soft-sphere force coefficient)
   double kbnd_d, R0sq_d, fang_d, e_bnd_coeff, e_ang_coeff;
   float pull_f;            // pulling force magnitude, kcal/mol/A
+  int dyn;                 // SOP_DYN_*
+  float a5;                // overdamped step factor h/zeta
+  double a5d, zeta_2h;     // the same in FP64; zeta/(2h) for the overdamped kinT
   int pull_i, pull_j;      // local indices of the pulled beads
   unsigned seed_lo, seed_hi;
   // run state (advanced by the prologue kernel)

@@ -25,6 +25,7 @@ LIST_NONE, LIST_NEIGHBOR, LIST_CELL, LIST_SKIN = 0, 1, 2, 3
 TERM_RANDOM, TERM_FENE, TERM_ANGLE, TERM_VDW, TERM_ALL = 1, 2, 4, 8, 15
 TUNE_SHAPE, TUNE_LISTS = 1, 2
 PREC_MIXED, PREC_FP64 = 0, 1
+DYN_UNDERDAMPED, DYN_OVERDAMPED = 0, 1
 
 
 class SopError(RuntimeError):
@@ -50,6 +51,7 @@ class Params(C.Structure):
         ("nnlup", C.c_int), ("nup", C.c_int), ("list_mode", C.c_int),
         ("force_terms", C.c_int), ("precision", C.c_int),
         ("pull_i", C.c_int), ("pull_j", C.c_int),
+        ("dynamics", C.c_int), ("a5", C.c_double),
     ]
 
 
@@ -131,6 +133,8 @@ _PROTOS = {
     "sop_last_run_timing": (C.c_int, [VP, DP, DP, C.POINTER(C.c_int64)]),
     "sop_profile_steps": (C.c_int, [VP, C.c_int64, DP, DP]),
     "sop_profile_steps_ex": (C.c_int, [VP, C.c_int64, DP]),
+    "sop_replica_checkpoint": (C.c_int, [VP, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "sop_replica_restore": (C.c_int, [VP, C.c_int, C.c_void_p, C.c_int64]),
     "sop_autotune": (C.c_int, [VP, C.c_int, C.c_char_p, C.c_int]),
     "sop_autotune_ex": (C.c_int, [VP, C.c_int, C.c_int, C.c_char_p, C.c_int]),
     "sop_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(VP)]),

@@ -26,8 +26,9 @@ def make_params(script=None, **kw) -> L.Params:
     p = L.default_params()
     if script is not None:
         sp = script_params(script)
-        for k in ("T", "zeta", "h", "a1", "a2", "a3", "a4", "boxl", "lcell", "ncell"):
+        for k in ("T", "zeta", "h", "a1", "a2", "a3", "a4", "a5", "boxl", "lcell", "ncell"):
             setattr(p, k, sp[k])
+        p.dynamics = L.DYN_OVERDAMPED if sp["sim_type"] == 2 else L.DYN_UNDERDAMPED
         p.nnlup = int(sp["nnlup"])
         p.nup = int(sp["nup"])
         p.seed = (-100 - int(sp["run"])) & 0xFFFFFFFFFFFFFFFF
@@ -145,6 +146,20 @@ class Engine:
         u = np.ascontiguousarray(unc_pos, np.float64)
         v = None if vel is None else np.ascontiguousarray(vel, np.float64)
         L.check(L.lib().sop_replica_set_state(self.h, r, L.dptr(u), L.dptr(v)), "sop_replica_set_state")
+
+    def checkpoint(self, r: int) -> bytes:
+        """Exact snapshot of replica r (sop_replica_checkpoint)."""
+        n = C.c_int64()
+        L.check(L.lib().sop_replica_checkpoint(self.h, r, None, 0, C.byref(n)), "sop_replica_checkpoint")
+        buf = C.create_string_buffer(n.value)
+        L.check(L.lib().sop_replica_checkpoint(self.h, r, buf, n.value, C.byref(n)),
+                "sop_replica_checkpoint")
+        return buf.raw
+
+    def restore(self, r: int, data: bytes):
+        """Continue replica r from a snapshot of the same system."""
+        buf = C.create_string_buffer(data, len(data))
+        L.check(L.lib().sop_replica_restore(self.h, r, buf, len(data)), "sop_replica_restore")
 
     def status(self, r: int):
         st = C.c_int()

@@ -183,6 +183,7 @@ def script_params(script) -> dict:
              nstep=5e7, run=1, neighborlist=0, celllist=0, sim_type=1)
     p["halfh"] = p["h"] / 2.0
     _integ(p)
+    p["a5"] = p["h"] / p["zeta"]  # params.cpp:392
     p["lcell"] = p["boxl"] / p["ncell"]
     for _, key, *val in script:
         v = val[0] if val else None
@@ -210,6 +211,7 @@ def script_params(script) -> dict:
             p["h"] = float(v)
             p["halfh"] = p["h"] / 2.0
             _integ(p)
+            p["a5"] = p["h"] / p["zeta"]
         elif key == "zeta":
             p["h"] = 2.5e-3 if p["sim_type"] == 1 else 0.02
             p["zeta"] = float(v)
@@ -217,11 +219,16 @@ def script_params(script) -> dict:
             p["a1"] = h * (1.0 - z * hh)
             p["a3"] = (1.0 - h * z / 2.0 + (h * z) * (h * z) / 4.0) / h
             p["a4"] = hh * (1.0 - h * z / 2.0)
+            p["a5"] = h / z
         elif key == "dynamics" and v == "underdamped":
             p["sim_type"] = 1
             p["h"] = 2.5e-3
             p["halfh"] = p["h"] / 2.0
             _integ(p)
+        elif key == "dynamics" and v == "overdamped":
+            p["sim_type"] = 2
+            p["h"] = 0.02
+            p["a5"] = p["h"] / p["zeta"]
     return p
 
 

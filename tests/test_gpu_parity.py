@@ -137,6 +137,33 @@ def test_noise_off_trajectory(eng, n, steps):
         eng.remove(r)
 
 
+@pytest.mark.parametrize("n,mode", [(76, "neighborlist"), (300, "celllist"), (1500, "neighborlist")])
+def test_overdamped_noise_off_trajectory(eng, n, mode):
+    """set dynamics overdamped: overdamped_iteration (sop.cpp:331-363) with
+    a5 = h/zeta, kinT from the increments (sop.cpp:270-278)."""
+    system = chain(n)
+    scr = [("set", "dynamics", "overdamped")] + script(mode)
+    r = eng.add(system, make_params(scr, force_terms=DET))
+    try:
+        port = port_for(system, scr)
+        assert port.param("sim_type") == 2
+        port.setup(True)
+        eng.run_plain(r, 1000)
+        port.run(1000)
+        _, x, _ = eng.state(r)
+        assert rmsd(x, port.coords(1)) < RMSD_TOL
+        for k in range(4):
+            np.testing.assert_array_equal(pairset(*eng.pairs(r, k)), pairset(*port.pairs(k)))
+        port.energy_eval()
+        e = eng.energy(r)
+        assert abs(e[5] - port.energy("rna_etot")) <= E_TOL * abs(port.energy("rna_etot"))
+        port.observables()
+        o = eng.observables(r)
+        assert abs(o[3] - port.energy("kinT")) <= 1e-3 * port.energy("kinT")
+    finally:
+        eng.remove(r)
+
+
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
 def test_golden_vectors(eng, path):
     g = np.load(path)

@@ -22,8 +22,9 @@ GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "sop
 needs_ref = pytest.mark.skipif(not O.ref_available(), reason="reference tree not built here")
 
 
-def golden_script(mode="neighborlist", temp="0.6", nstep=100, nup=50):
-    return [("set", "zeta", "50"), ("set", "t_step", "0.05"), ("set", "temp", temp),
+def golden_script(mode="neighborlist", temp="0.6", nstep=100, nup=50, dynamics=None):
+    pre = [("set", "dynamics", dynamics)] if dynamics else []
+    return pre + [("set", "zeta", "50"), ("set", "t_step", "0.05"), ("set", "temp", temp),
             ("set", "nstep", str(nstep)), ("set", "nup", str(nup)),
             ("set", "cutofftype", mode), ("set", "nnlup", "10"), ("set", "boxl", "500"),
             ("set", "ncell", "62.5"), ("set", "run", "1")]
@@ -49,13 +50,16 @@ def pairs(o, k):
 
 
 @needs_ref
-@pytest.mark.parametrize("n,mode", [(30, "neighborlist"), (76, "neighborlist"), (76, "celllist"),
-                                    (120, "none"), (250, "neighborlist")])
-def test_port_equals_reference(n, mode):
+@pytest.mark.parametrize("n,mode,dyn", [(30, "neighborlist", None), (76, "neighborlist", None),
+                                        (76, "celllist", None), (120, "none", None),
+                                        (250, "neighborlist", None),
+                                        (76, "neighborlist", "overdamped"),
+                                        (150, "celllist", "overdamped")])
+def test_port_equals_reference(n, mode, dyn):
     system = S.synth_chain(5000 + n, n)
     ref, port = O.Ref(), O.Port()
     with tempfile.TemporaryDirectory() as d:
-        path = S.write_reference_files(system, d, golden_script(mode), run=False)
+        path = S.write_reference_files(system, d, golden_script(mode, dynamics=dyn), run=False)
         cwd = os.getcwd()
         os.chdir(d)
         try:
