@@ -257,6 +257,8 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
     CK(dalloc(&A.stage[b], 2 * cap));
   }
   CK(dalloc(&A.incr, 3 * cap));
+  CK(dalloc(&A.incr64, 3 * cap));
+  CK(cudaMemsetAsync(A.incr64, 0, 3 * cap * sizeof(double), e->stream));
   CK(dalloc(&A.vel, 3 * cap));
   CK(dalloc(&A.force, 3 * cap));
   CK(dalloc(&A.xb, cap));
@@ -323,8 +325,10 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   upload_tables(tables(), e->stream);
   CK(cudaGetLastError());
   CK(init_kernels((int)e->prop.sharedMemPerBlockOptin, (int)e->prop.sharedMemPerMultiprocessor));
-  CK(dalloc(&e->d_counts, 2));
-  CK(cudaMemsetAsync(e->d_counts, 0, 2 * sizeof(int), e->stream));
+  CK(dalloc(&e->d_counts, 3));
+  CK(cudaMemsetAsync(e->d_counts, 0, 3 * sizeof(int), e->stream));
+  e->items64_cap = cap / 256 + cfg.max_replicas + 16;
+  CK(dalloc(&e->d_items64, e->items64_cap));
   CK(dalloc(&e->d_pack_xyz, 3 * cap));
   CK(dalloc(&e->d_pack_vel, 3 * cap));
   CK(dalloc(&e->d_pack_ids, cfg.max_replicas));
@@ -348,10 +352,10 @@ extern "C" int sop_engine_destroy(sop_engine* e) {
   cudaStreamSynchronize(e->stream);
   if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
   DevArrays& A = e->A;
-  void* ptrs[] = {A.X[0], A.X[1], A.stage[0], A.stage[1], A.incr, A.vel, A.force, A.xb, A.topo,
+  void* ptrs[] = {A.X[0], A.X[1], A.stage[0], A.stage[1], A.incr, A.incr64, A.vel, A.force, A.xb, A.topo,
                   A.exc_rng, A.nl_cnt, A.nl, A.nat, A.nat_r0, A.bnd, A.bnd_r0, A.ang, A.exc,
                   A.rep, A.pairs_out, A.pairs_cnt, A.err, A.units, A.unit_cnt, A.slice_done,
-                  A.done_list, A.done_cnt, e->d_ids, e->d_items, e->d_counts, e->d_pack_xyz,
+                  A.done_list, A.done_cnt, e->d_ids, e->d_items, e->d_items64, e->d_counts, e->d_pack_xyz,
                   e->d_pack_vel, e->d_pack_ids, e->d_pack_off, A.bin_p, A.bin_sorted,
                   A.bin_cell, A.cstart, A.ccur, A.bin_hdr, A.step_ctr};
   for (void* p : ptrs) cudaFree(p);
@@ -392,6 +396,8 @@ static int fill_repdev(const sop_params& p, RepDev& d) {
   d.a1d = p.a1; d.a2d = p.a2; d.a3d = p.a3; d.a4d = p.a4;
   double amp = (p.h > 0 && p.T > 0 && p.zeta > 0) ? std::sqrt(2.0 * p.T * p.zeta / p.h) : 0.0;
   d.noise_amp = (float)amp;  // random_force (energy.cpp:456)
+  d.noise_amp_d = amp;
+  d.pull_fd = p.pull_force;
   d.T = (float)p.T;
   if (p.T < kEpsT && p.T != 0.0) d.T = 0.0f;  // keep the sop.cpp:316 branch exact
   d.kbnd = (float)p.k_bnd;
@@ -413,7 +419,7 @@ static int fill_repdev(const sop_params& p, RepDev& d) {
   d.seed_hi = (uint32_t)(p.seed >> 32);
   if (p.list_mode < SOP_LIST_NONE || p.list_mode > SOP_LIST_SKIN) return SOP_ERR_ARG;
   if (p.dynamics != SOP_DYN_UNDERDAMPED && p.dynamics != SOP_DYN_OVERDAMPED) return SOP_ERR_ARG;
-  if (p.precision != SOP_PREC_MIXED) return SOP_ERR_UNSUPPORTED;
+  if (p.precision != SOP_PREC_MIXED && p.precision != SOP_PREC_FP64) return SOP_ERR_ARG;
   return SOP_OK;
 }
 
@@ -891,6 +897,9 @@ extern "C" int sop_replica_set_params(sop_engine* e, int r, const sop_params* p)
   if (rc) return rc;
   Replica& R = e->reps[r];
   bool mode_changed = cfg.mode != d.mode || p->skin != R.params.skin;
+  // another precision moves the replica to the other step kernel's items (the
+  // next run restarts from the stored velocities, so no increment carries over)
+  if (cfg.prec != d.prec) e->layout_dirty = true;
   // configuration fields only; run state and layout stay
   d.mode = cfg.mode; d.terms = cfg.terms; d.prec = cfg.prec; d.nnlup = cfg.nnlup; d.nup = cfg.nup;
   d.skin = cfg.skin; d.cell_edge = cfg.cell_edge; d.half_skin2 = cfg.half_skin2;
@@ -898,6 +907,7 @@ extern "C" int sop_replica_set_params(sop_engine* e, int r, const sop_params* p)
   d.a1 = cfg.a1; d.a2 = cfg.a2; d.a3 = cfg.a3; d.a4 = cfg.a4;
   d.a1d = cfg.a1d; d.a2d = cfg.a2d; d.a3d = cfg.a3d; d.a4d = cfg.a4d;
   d.noise_amp = cfg.noise_amp; d.T = cfg.T; d.kbnd = cfg.kbnd; d.R0sq = cfg.R0sq;
+  d.noise_amp_d = cfg.noise_amp_d; d.pull_fd = cfg.pull_fd;
   d.inv_R0sq = cfg.inv_R0sq;
   d.kbnd_d = cfg.kbnd_d; d.R0sq_d = cfg.R0sq_d; d.fang = cfg.fang; d.fang_d = cfg.fang_d;
   d.e_bnd_coeff = cfg.e_bnd_coeff; d.e_ang_coeff = cfg.e_ang_coeff; d.pull_f = cfg.pull_f;
@@ -1011,10 +1021,12 @@ extern "C" int sop_replica_info(sop_engine* e, int r, int64_t* out) {
 
 // Step-kernel work items of one replica: chunks of cfg.chunk_beads beads,
 // staged through shared memory when the replica fits the stage limit.
+// FP64-precision replicas: chunks of 256 beads for k_step64 (never staged).
 static std::vector<StepItem> replica_items(const sop_engine* e, int r) {
   const Replica& R = e->reps[r];
-  const int chunk = e->cfg.chunk_beads;
-  const int staged = e->cfg.stage_limit > 0 && R.n <= e->cfg.stage_limit;
+  const bool fp64 = R.params.precision == SOP_PREC_FP64;
+  const int chunk = fp64 ? 256 : e->cfg.chunk_beads;
+  const int staged = !fp64 && e->cfg.stage_limit > 0 && R.n <= e->cfg.stage_limit;
   std::vector<StepItem> items;
   for (int b = 0; b < R.n; b += chunk) items.push_back(StepItem{r, b, std::min(R.n, b + chunk), staged});
   return items;
@@ -1029,28 +1041,40 @@ int sop::refresh_layout(sop_engine* e) {
   e->active = ids;
   e->max_n = 0;
   e->items.clear();
+  e->items64.clear();
   for (int r : ids) {
     const Replica& R = e->reps[r];
     e->max_n = std::max(e->max_n, R.n);
     std::vector<StepItem> it = replica_items(e, r);
-    e->items.insert(e->items.end(), it.begin(), it.end());
+    auto& dst = R.params.precision == SOP_PREC_FP64 ? e->items64 : e->items;
+    dst.insert(dst.end(), it.begin(), it.end());
   }
   if ((long long)e->items.size() + 64 > e->items_cap) return SOP_ERR_FULL;
-  // the kernels read the counts from device memory, so a captured graph stays valid
-  const int counts[2] = {(int)ids.size(), (int)e->items.size()};
+  if ((long long)e->items64.size() > e->items64_cap) return SOP_ERR_FULL;
+  // the kernels read the counts from device memory, so a captured graph stays
+  // valid; only the first FP64 replica (one more kernel per step) needs a recapture
+  const int counts[3] = {(int)ids.size(), (int)e->items.size(), (int)e->items64.size()};
   if (!ids.empty()) CK(h2d(e->d_ids, ids.data(), ids.size(), e->stream));
   if (!e->items.empty()) CK(h2d(e->d_items, e->items.data(), e->items.size(), e->stream));
-  CK(h2d(e->d_counts, counts, 2, e->stream));
+  if (!e->items64.empty()) CK(h2d(e->d_items64, e->items64.data(), e->items64.size(), e->stream));
+  CK(h2d(e->d_counts, counts, 3, e->stream));
+  const bool has64 = !e->items64.empty();
+  if (has64 && !e->has64) e->graph_valid = false;
+  e->has64 = e->has64 || has64;
   e->layout_dirty = false;
   return SOP_OK;
 }
 
 // One step over given ids / items with host counts (single-replica paths).
 int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items,
-                      int nitems, int max_staged, int step_grid, int pro_grid) {
+                      int nitems, int max_staged, int step_grid, int pro_grid, bool fp64) {
   CK(launch_prologue(e->A, d_ids, nrep, nullptr, 0, 0, pro_grid, e->stream));
-  CK(launch_step(e->A, d_items, nitems, nullptr, max_staged, e->cfg.lanes_per_bead,
-                 e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads, step_grid, e->stream));
+  if (fp64)
+    CK(launch_step64(e->A, d_items, nitems, nullptr, step_grid, e->stream));
+  else
+    CK(launch_step(e->A, d_items, nitems, nullptr, max_staged, e->cfg.lanes_per_bead,
+                   e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads, step_grid,
+                   e->stream));
   e->launches += kStepLaunches;
   return SOP_OK;
 }
@@ -1061,8 +1085,14 @@ int sop::enqueue_batched_step(sop_engine* e) {
   CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0,
                      e->pro_grid, e->stream));
   CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, e->max_staged,
-                 e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads, e->step_grid, e->stream));
+                 e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy,
+                 e->cfg.block_threads, e->step_grid, e->stream));
   e->launches += kStepLaunches;
+  if (e->has64) {  // FP64-precision replicas, after the mixed ones
+    CK(launch_step64(e->A, e->d_items64, (int)e->items64_cap, e->d_counts + 2, e->pro_grid,
+                     e->stream));
+    e->launches++;
+  }
   return SOP_OK;
 }
 
@@ -1114,7 +1144,7 @@ extern "C" int sop_run_plain(sop_engine* e, int r, int64_t nsteps) {
                              2 * e->prop.multiProcessorCount);
   for (int64_t s = 0; s <= nsteps; s++) {
     int rc = enqueue_step(e, e->d_ids + id_slot, 1, e->d_items + item_slot, (int)items.size(),
-                          staged ? R.n : 0, grid, bgrid);
+                          staged ? R.n : 0, grid, bgrid, R.params.precision == SOP_PREC_FP64);
     if (rc) return rc;
   }
   // observables are computed on demand (sop_observables), not at run end
@@ -1451,9 +1481,13 @@ static int run_phase(sop_engine* e, int r, int phase) {
   const long long item_slot = e->items_cap - (long long)items.size();
   CK(h2d(e->d_items + item_slot, items.data(), items.size(), e->stream));
   k_set_phase<<<1, 1, 0, e->stream>>>(e->A.rep, r, phase);
-  CK(launch_step(e->A, e->d_items + item_slot, (int)items.size(), nullptr, staged ? R.n : 0,
-                 e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads,
-                 std::min((int)items.size(), 4 * e->prop.multiProcessorCount), e->stream));
+  const int grid = std::min((int)items.size(), 4 * e->prop.multiProcessorCount);
+  if (R.params.precision == SOP_PREC_FP64)
+    CK(launch_step64(e->A, e->d_items + item_slot, (int)items.size(), nullptr, grid, e->stream));
+  else
+    CK(launch_step(e->A, e->d_items + item_slot, (int)items.size(), nullptr, staged ? R.n : 0,
+                   e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy,
+                   e->cfg.block_threads, grid, e->stream));
   e->launches += 2;
   CK(cudaStreamSynchronize(e->stream));
   return check_errors(e);

@@ -65,6 +65,10 @@ struct sop_engine {
   long long items_cap = 0;
   std::vector<int> active;
   std::vector<sop::StepItem> items;
+  sop::StepItem* d_items64 = nullptr;  // items of FP64-precision replicas (k_step64)
+  std::vector<sop::StepItem> items64;
+  long long items64_cap = 0;
+  bool has64 = false;                  // an FP64 replica was ever laid out (k_step64 launched)
   int max_n = 0, max_staged = 0, step_grid = 1, pro_grid = 1;
   int* d_counts = nullptr;          // {active replicas, work items}, read by the kernels
   // packed host-order state of sop_run_host (one copy each way)
@@ -112,7 +116,7 @@ LaunchShape get_launch_shape(const sop_engine* e);
 // recompute the persistent grid, invalidate layout and graph
 void set_launch_shape(sop_engine* e, const LaunchShape& s);
 int enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items, int nitems,
-                 int max_staged, int step_grid, int pro_grid);
+                 int max_staged, int step_grid, int pro_grid, bool fp64);
 // one step of every active replica, sized only by device-resident counts
 int enqueue_batched_step(sop_engine* e);
 int run_batched(sop_engine* e, int64_t nsteps, bool timed);

@@ -1120,6 +1120,184 @@ __global__ void __launch_bounds__(256, MB) k_step_w(DevArrays A, const StepItem*
 }
 
 // ---------------------------------------------------------------------------------
+// K3+K4 in FP64 (replicas with precision SOP_PREC_FP64): one thread per bead,
+// positions, forces and the update in double precision with the reference's
+// formulas (energy.cpp:259-447, sop.cpp:282-363), pair-list decisions exact as
+// in the mixed kernel, contributions summed in int64 fixed point (2^-40) so
+// that the sums do not depend on list order.  The drift / force-error
+// reference for the mixed-precision path.
+
+__device__ __forceinline__ long long fix40(double v) { return __double2ll_rn(v * 1099511627776.0); }
+
+__device__ void step_bead64(const DevArrays& A, const ItemCtx& C, const RepDev* R, int i) {
+  const long long g = (long long)C.off + i, cap = A.cap;
+  const double* X = A.X[C.cur];
+  const double xi = X[g], yi = X[cap + g], zi = X[2 * cap + g];
+  const int ti = (int)f2u(A.stage[C.cur][2 * g].w);
+  const int4 tp = A.topo[g];
+  const int nat_cnt = tp.w & 0xFFFF, bnd_cnt = (tp.w >> 16) & 0xFF, ang_cnt = (tp.w >> 24) & 0xFF;
+  const bool upd = (C.phase == PH_FIRST || C.phase == PH_NORMAL) && C.mode != SOP_LIST_NONE;
+  long long Fx = 0, Fy = 0, Fz = 0;
+  double mag = 0.0;
+  int st = 0;
+  auto add = [&](double cx, double cy, double cz) {
+    Fx += fix40(cx);
+    Fy += fix40(cy);
+    Fz += fix40(cz);
+    mag += fabs(cx) + fabs(cy) + fabs(cz);
+  };
+  auto delta = [&](int j, double& dx, double& dy, double& dz) {
+    const long long gj = (long long)C.off + j;
+    dx = __dsub_rn(X[gj], xi);
+    dy = __dsub_rn(X[cap + gj], yi);
+    dz = __dsub_rn(X[2 * cap + gj], zi);
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  };
+  if (C.terms & SOP_TERM_VDW) {
+    for (int k = 0; k < nat_cnt; k++) {  // native attraction (energy.cpp:274-311)
+      const int4 e = A.nat[tp.x + k];
+      const int j = e.x & (int)kIdx;
+      double dx, dy, dz;
+      const double d2 = delta(j, dx, dy, dz);
+      const double r0 = A.nat_r0[tp.x + k], r2 = r0 * r0;
+      if (e.x & (int)kPL) {
+        if (!(d2 < kTol * r2)) {
+          const int tj = (int)f2u(A.stage[C.cur][2 * ((long long)C.off + j)].w);
+          const double r6 = r2 * r2 * r2, r12 = r6 * r6;
+          const double d6 = d2 * d2 * d2, d12 = d6 * d6;
+          const double co = c_ff.force_coeff_att[ti][tj] / d2 * ((r12 / d12) - (r6 / d6));
+          add(co * dx, co * dy, co * dz);
+        }
+      }
+      if (upd) {
+        const double rc = 2.5 * r0;  // sop.cpp:504-506
+        const bool plb = (e.x & (int)kNL) && d2 < rc * rc;
+        if (plb != ((e.x & (int)kPL) != 0)) A.nat[tp.x + k].x = e.x ^ (int)kPL;
+      }
+    }
+    const int cnt = A.nl_cnt[g];
+    const long long row = C.nl_base + (long long)i * C.L;
+    for (int k = 0; k < cnt; k++) {  // non-native repulsion (energy.cpp:313-350)
+      const int e = A.nl[row + k];
+      const int j = e & (int)kIdx;
+      double dx, dy, dz;
+      const double d2 = delta(j, dx, dy, dz);
+      const int tj = (int)f2u(A.stage[C.cur][2 * ((long long)C.off + j)].w);
+      if (e & (int)kPL) {
+        if (!(d2 < c_ff.sigma_rep2[ti][tj] * kTol)) {
+          const double d6 = d2 * d2 * d2, d12 = d6 * d6;
+          const double co = c_ff.force_coeff_rep[ti][tj] / d2 *
+                            (2.0 * c_ff.sigma_rep12[ti][tj] / d12 + c_ff.sigma_rep6[ti][tj] / d6);
+          add(co * dx, co * dy, co * dz);
+        }
+      }
+      if (upd) {
+        const bool plb = d2 < c_ff.rc2_pl[ti][tj];
+        if (plb != ((e & (int)kPL) != 0)) A.nl[row + k] = e ^ (int)kPL;
+      }
+    }
+  }
+  if (C.terms & SOP_TERM_FENE) {
+    for (int k = 0; k < bnd_cnt; k++) {  // FENE (energy.cpp:402-447)
+      const int j = A.bnd[tp.y + k].x;
+      double dx, dy, dz;
+      const double d = sqrt(delta(j, dx, dy, dz));
+      const double dev = d - A.bnd_r0[tp.y + k];
+      const double den = 1.0 - dev * dev / R->R0sq_d;
+      if (!(den > 0.0)) st |= SOP_ST_FENE;
+      const double temp = -R->kbnd_d * dev / d / den;
+      add(-temp * dx, -temp * dy, -temp * dz);
+    }
+  }
+  if (C.terms & SOP_TERM_ANGLE) {
+    for (int k = 0; k < ang_cnt; k++) {  // i,i+2 soft sphere (energy.cpp:354-400)
+      const int j = A.ang[tp.z + k];
+      double dx, dy, dz;
+      const double d2 = delta(j, dx, dy, dz);
+      const double d4 = d2 * d2, d8 = d4 * d4;
+      const double co = R->fang_d / d8;
+      add(-co * dx, -co * dy, -co * dz);
+    }
+  }
+  if (!(mag <= (double)kFixMax)) st |= SOP_ST_NONFINITE;
+  double F[3] = {(double)Fx * 9.094947017729282e-13, (double)Fy * 9.094947017729282e-13,
+                 (double)Fz * 9.094947017729282e-13};  // 2^-40
+  if ((C.terms & SOP_TERM_RANDOM) && R->noise_amp_d > 0.0) {
+    float nrm[3];
+    bead_normals(C.seed_lo, C.seed_hi, C.t_cur, i, nrm);
+    for (int c = 0; c < 3; c++) F[c] += R->noise_amp_d * (double)nrm[c];
+  }
+  if (C.pull_f != 0.f && (i == C.pull_i || i == C.pull_j)) {
+    const int o = (i == C.pull_i) ? C.pull_j : C.pull_i;
+    double ux, uy, uz;
+    const double inv = 1.0 / sqrt(delta(o, ux, uy, uz));
+    const double pf = R->pull_fd;
+    F[0] -= pf * ux * inv; F[1] -= pf * uy * inv; F[2] -= pf * uz * inv;
+  }
+  if (C.phase == PH_FORCE || C.phase == PH_FINAL)
+    for (int c = 0; c < 3; c++) A.force[c * cap + g] = F[c];
+  if (C.phase != PH_FORCE) {
+    double inc[3];
+    if (C.dyn == SOP_DYN_OVERDAMPED) {
+      if (C.phase != PH_FIRST && (C.out || C.phase == PH_FINAL))
+        for (int c = 0; c < 3; c++) A.vel[c * cap + g] = A.incr64[c * cap + g];
+      for (int c = 0; c < 3; c++) inc[c] = R->a5d * F[c];
+    } else {
+      const bool keepv = (C.phase == PH_FIRST) || (C.T < (float)kEpsT);
+      double v[3];
+      for (int c = 0; c < 3; c++)
+        v[c] = keepv ? A.vel[c * cap + g] : R->a3d * A.incr64[c * cap + g] + R->a4d * F[c];
+      if (!keepv && (C.out || C.phase == PH_FINAL))
+        for (int c = 0; c < 3; c++) A.vel[c * cap + g] = v[c];
+      for (int c = 0; c < 3; c++) inc[c] = R->a1d * v[c] + R->a2d * F[c];
+    }
+    if (C.phase != PH_FINAL) {
+      const int nb = C.cur ^ 1;
+      const double xo[3] = {xi, yi, zi};
+      float h[3], l[3];
+      double xn[3];
+      for (int c = 0; c < 3; c++) {
+        xn[c] = xo[c] + inc[c];
+        A.X[nb][c * cap + g] = xn[c];
+        A.incr64[c * cap + g] = inc[c];
+        A.incr[c * cap + g] = (float)inc[c];
+        split_double(xn[c], h[c], l[c]);
+      }
+      const float4 hi = A.stage[C.cur][2 * g], lo = A.stage[C.cur][2 * g + 1];
+      A.stage[nb][2 * g] = make_float4(h[0], h[1], h[2], hi.w);
+      A.stage[nb][2 * g + 1] = make_float4(l[0], l[1], l[2], lo.w);
+      if (C.mode == SOP_LIST_SKIN) {
+        const float4 b = A.xb[g];
+        const float ex = h[0] - b.x, ey = h[1] - b.y, ez = h[2] - b.z;
+        const float d2 = ex * ex + ey * ey + ez * ez;
+        if (d2 > C.half_skin2) {
+          A.rep[C.r].rebuild = 1;
+          *A.any_rebuild = 1;
+        } else if (d2 > C.half_skin2 * A.group_frac2) {
+          A.rep[C.r].near = 1;
+        }
+      }
+      if (!(isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]))) st |= SOP_ST_NONFINITE;
+    }
+  }
+  if (!(isfinite(F[0]) && isfinite(F[1]) && isfinite(F[2]))) st |= SOP_ST_NONFINITE;
+  if (st) atomicOr(&A.rep[C.r].status, st);
+}
+
+// One CTA per work item, one thread per bead.
+__global__ void __launch_bounds__(256) k_step64(DevArrays A, const StepItem* items,
+                                                const int* nitems_dev, int nitems_host) {
+  const int nitems = nitems_dev ? *nitems_dev : nitems_host;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const StepItem w = items[it];
+    const ItemCtx C = load_ctx(A, w.r);
+    if (C.phase == PH_SKIP) continue;
+    for (int b = w.b0 + (int)threadIdx.x; b < w.b1; b += (int)blockDim.x)
+      step_bead64(A, C, &A.rep[w.r], b);
+  }
+}
+
+// ---------------------------------------------------------------------------------
 // K5: energies in FP64 (energy.cpp:115-257), deterministic fixed-order sums
 
 __device__ void block_sum(double* v, int nv, double* red) {
@@ -1475,6 +1653,14 @@ int step_blocks_per_sm(int lanes, int min_blocks, int strategy, int threads, int
     return 1;
   }
   return n > 0 ? n : 1;
+}
+
+cudaError_t launch_step64(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
+                          int grid, cudaStream_t s) {
+  if (nitems <= 0) return cudaSuccess;
+  if (grid <= 0) grid = nitems;
+  k_step64<<<grid, 256, 0, s>>>(A, items, nitems_dev, nitems);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s) {

@@ -12,6 +12,7 @@ struct DevArrays {
   double* X[2];       // SoA unc_pos, x|y|z blocks of `cap`
   float4* stage[2];   // {hi.xyz,type},{lo.xyz,chain} per bead
   float* incr;        // SoA position increment of the last step
+  double* incr64;     // the same in FP64 (replicas with FP64 precision)
   double* vel;        // SoA velocities
   double* force;      // SoA forces of the last force-only / final step
   float4* xb;         // positions at the last list build
@@ -100,6 +101,9 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, co
 cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
                         int max_staged, int lanes, int min_blocks, int strategy, int threads,
                         int grid, cudaStream_t s);
+// the FP64-precision step over its own items (one thread per bead)
+cudaError_t launch_step64(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
+                          int grid, cudaStream_t s);
 cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s);
 cudaError_t launch_observables(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s);
 cudaError_t launch_pairlist(const DevArrays& A, int r, int off, int n, cudaStream_t s);

@@ -60,6 +60,7 @@ struct RepDev {
   float a1, a2, a3, a4;    // FP32 integrator constants
   double a1d, a2d, a3d, a4d;
   float noise_amp;         // sqrt(2 T zeta / h)
+  double noise_amp_d, pull_fd;  // the same and the pulling force in FP64
   float T;
   float kbnd, R0sq, inv_R0sq;  // FENE
   float fang;              // 6 eps sigma_ss^6 (soft-sphere force coefficient)
