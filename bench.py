@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-steps", default="100,10000", help="log-uniform step-count range")
     ap.add_argument("--serve-chunk", type=int, default=100)
+    ap.add_argument("--large-chains", type=int, default=100,
+                    help="single large system: chains x --large-len beads (0 = skip)")
+    ap.add_argument("--large-len", type=int, default=500)
+    ap.add_argument("--large-steps", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -201,6 +205,49 @@ def algorithmic_bytes(eng, ids, systems):
 
 
 PN_PER_KCAL_MOL_A = 69.48
+
+
+def large_system(args):
+    """100 chains x 500 beads in one compact globule (50,000 beads), skin
+    lists: mixed-precision throughput; the same system in FP64 precision
+    (the drift reference): its throughput, the mixed-vs-FP64 force error at
+    the start and how far the total energies drift apart over the run (same
+    seed and noise stream)."""
+    from sop_gb300 import _lib as L
+    from sop_gb300 import systems as S
+    from sop_gb300.engine import Engine, make_params
+    s = S.synth_globule(3000, args.large_chains, args.large_len)
+    n = s.nbead
+    steps, nup = args.large_steps, max(1, args.large_steps // 4)
+    sc = [c if c[1] != "nup" else ("set", "nup", str(nup)) for c in workload_script()]
+    out = {"workload": "%d chains x %d beads, one globule (%d beads), skin lists, T 0.6"
+                       % (args.large_chains, args.large_len, n), "steps": steps}
+    energies = {}
+    with Engine(0, max_beads=2 * n + 4096, max_replicas=4, max_list_entries=n * 400) as eng:
+        for prec in (L.PREC_MIXED, L.PREC_FP64):
+            key = "fp64" if prec == L.PREC_FP64 else "mixed"
+            r = eng.add(s, make_params(sc, seed=31337, list_mode="skin", skin=2.0, precision=prec))
+            if prec == L.PREC_MIXED:
+                f_mixed = eng.force(r)
+            else:
+                f64 = eng.force(r)
+                out["force_rel_err_mixed_vs_fp64"] = float(
+                    np.linalg.norm(f_mixed - f64) / np.linalg.norm(f64))
+            eng.run(20)  # warm
+            trace = []
+            total = 0.0
+            for _ in range(4):
+                eng.run(nup)
+                total += eng.timing()[0]
+                trace.append(float(eng.energy(r)[5]))
+            energies[key] = trace
+            out[key + "_bead_steps_per_s"] = n * 4 * nup / (total / 1e3)
+            eng.remove(r)
+    e_m, e_d = np.array(energies["mixed"]), np.array(energies["fp64"])
+    out["etot_fp64"] = energies["fp64"]
+    out["etot_mixed"] = energies["mixed"]
+    out["energy_drift_rel_max"] = float(np.max(np.abs(e_m - e_d) / np.abs(e_d)))
+    return out
 
 
 def serve_stream(args, rank):
@@ -378,6 +425,7 @@ def run_gb300(args):
     ferr = force_check(eng, ids, systems)
     eng.close()
     served = serve_stream(args, rank) if args.serve_seconds > 0 else None
+    large = large_system(args) if (args.large_chains > 0 and rank == 0) else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -396,6 +444,7 @@ def run_gb300(args):
         "plain_gpu_path": {"value": plain, "unit": UNIT, "steps": args.plain_steps,
                            "batched_over_plain": value / plain},
         "served": served,
+        "large_system": large,
         "force_rel_err": ferr,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
