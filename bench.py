@@ -82,7 +82,22 @@ def workload_script():
             ("set", "nnlup", "10"), ("set", "boxl", "2000"), ("set", "ncell", "250"), ("set", "run", "1")]
 
 
+def job_totals(units, seconds, world, device="cpu"):
+    """Whole-job figures of a replicas-only run: the units all ranks processed
+    (sum) and the job's time (max over ranks)."""
+    if world == 1:
+        return float(units), float(seconds)
+    import torch
+    import torch.distributed as dist
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(u.item()), float(t.item())
+
+
 def build_workload(args, rank):
+    """Each rank its own seeded mix (replicas only: no data is shared)."""
     from sop_gb300 import systems as S
     systems, temps = S.mixed_batch(args.replicas, args.lo, args.hi, seed=2000 + 100000 * rank)
     return systems, temps
@@ -382,11 +397,9 @@ def run_gb300(args):
             times.append(eng.timing()[0])
     launches = eng.launches() - l0  # every kernel the engine launched in the timed region
     total_ms = sum(times)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = beads * md * args.steps * world / (total_ms / 1e3)
+    units, total_s = job_totals(beads * md * args.steps, total_ms / 1e3, world, "cuda")
+    total_ms = total_s * 1e3
+    value = units / total_s
 
     # roofline of the fused step kernel
     step_ms, pro_ms = eng.profile_steps(md)
@@ -409,11 +422,14 @@ def run_gb300(args):
     e2e_steps = max(2, args.steps // 2)
     eng.run_host(xin, vin, md, xout, vout)  # warm
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         eng.run_host(xin, vin, md, xout, vout)
     e2e_s = time.perf_counter() - t0
-    e2e = beads * md * e2e_steps * world / e2e_s
+    e2e_units, e2e_s = job_totals(beads * md * e2e_steps, e2e_s, world, "cuda")
+    e2e = e2e_units / e2e_s
 
     # the plain one-system-per-launch path over the same mix
     t0 = time.perf_counter()
