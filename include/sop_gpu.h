@@ -219,6 +219,16 @@ int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_kernel_ms, dou
  * k_build (list slices, energies, observables), ms[3] k_step. */
 int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms);
 
+/* The energies the last output step computed (step t with t % nup == 0 or the
+ * final step of a run window), with the pair list that step's force used, as
+ * the reference's energy_eval at an nup step (sop.cpp:174-181); also the
+ * stored observables.  Either pointer may be NULL. */
+int sop_replica_outputs(sop_engine* e, int replica, double* energy6, double* obs5);
+/* Set the step counter (the force-evaluation index that keys the noise
+ * stream) of a replica between runs, e.g. to istep_restart on a restart
+ * (sop.cpp:132-140). */
+int sop_replica_set_step(sop_engine* e, int replica, int64_t step);
+
 /* ---- checkpoint / restart ------------------------------------------------------ */
 /* Exact snapshot of one replica (both position buffers, increments,
  * velocities, list rows with their pair-list bits, native flags, skin

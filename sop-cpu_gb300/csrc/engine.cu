@@ -1535,6 +1535,26 @@ extern "C" int sop_observables(sop_engine* e, int r, double* out) {
   return SOP_OK;
 }
 
+extern "C" int sop_replica_outputs(sop_engine* e, int r, double* energy6, double* obs5) {
+  if (!e || !live(e, r)) return SOP_ERR_ARG;
+  RepDev d;
+  int rc = get_rep(e, r, &d);
+  if (rc) return rc;
+  if (energy6) std::memcpy(energy6, d.energy, sizeof d.energy);
+  if (obs5) std::memcpy(obs5, d.obs, sizeof d.obs);
+  return SOP_OK;
+}
+
+extern "C" int sop_replica_set_step(sop_engine* e, int r, int64_t step) {
+  if (!e || !live(e, r) || step < 0) return SOP_ERR_ARG;
+  RepDev d;
+  int rc = get_rep(e, r, &d);
+  if (rc) return rc;
+  if (d.running) return SOP_ERR_STATE;
+  d.t = step;
+  return put_rep(e, r, d);
+}
+
 extern "C" int sop_underdamped_iteration(sop_engine* e, int r) {
   // incr = a1 v + a2 F, x += incr, F = force(x), v = a3 incr + a4 F: a run of one
   // iteration (the restart step recomputes F at x with the same noise index)

@@ -133,6 +133,8 @@ _PROTOS = {
     "sop_last_run_timing": (C.c_int, [VP, DP, DP, C.POINTER(C.c_int64)]),
     "sop_profile_steps": (C.c_int, [VP, C.c_int64, DP, DP]),
     "sop_profile_steps_ex": (C.c_int, [VP, C.c_int64, DP]),
+    "sop_replica_outputs": (C.c_int, [VP, C.c_int, DP, DP]),
+    "sop_replica_set_step": (C.c_int, [VP, C.c_int, C.c_int64]),
     "sop_replica_checkpoint": (C.c_int, [VP, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "sop_replica_restore": (C.c_int, [VP, C.c_int, C.c_void_p, C.c_int64]),
     "sop_autotune": (C.c_int, [VP, C.c_int, C.c_char_p, C.c_int]),
