@@ -309,6 +309,7 @@ def serve_stream(args, rank):
         if pending == 0 and nxt < nreq:
             time.sleep(max(0.0, min(0.005, arrivals[nxt] - (srv.clock() - t_start))))
     done += srv.poll()
+    phases = srv.timing()
     srv.close()
     lat = np.array([r["finish"] - r["submit"] for r in done])
     svc = np.array([r["finish"] - r["start"] for r in done])
@@ -318,7 +319,7 @@ def serve_stream(args, rank):
     return {"value": work / span, "unit": UNIT, "requests": len(done), "window_s": float(arrivals[-1]),
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "p50_service_s": float(np.percentile(svc, 50)), "p99_service_s": float(np.percentile(svc, 99)),
-            "offered_bead_steps_per_s": offered,
+            "offered_bead_steps_per_s": offered, "pump_phases_s": phases,
             "errors": int(sum(1 for r in done if r["status"] or r["replica_status"])),
             "stream": "Poisson %.0f req/s, N log-uniform 30-5000 (pool of %d seeded chains), steps "
                       "log-uniform %g-%g (the 1e4-1e6 of the serving config scaled by 1/100 so requests "

@@ -158,6 +158,26 @@ int sop_engine_launches(const sop_engine* e, int64_t* launches);
 /* Upload a system; builds its lists at the initial positions (the set-up of
  * underdamped_ctrl, sop.cpp:117-125) and evaluates nothing else. */
 int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* replica);
+
+/* Admission in two halves, for servers: sop_prepare does the host work
+ * (topology, row sizing, device bytes) without touching any device, so it
+ * can run while the GPU steps other replicas; sop_replicas_admit places
+ * prepared systems in order until a slot or an arena is missing (*admitted
+ * of them; SOP_ERR_FULL if none), builds all their lists in one launch and,
+ * when nsteps is given, opens each one's run window of nsteps[k] steps
+ * (as sop_replica_start).  A prepared system may be admitted any number of
+ * times (to any engine) and is released with sop_prepared_free. */
+typedef struct sop_prepared sop_prepared;
+int sop_prepare(const sop_system_desc* d, sop_prepared** out);
+int sop_prepared_bytes(const sop_prepared* p, int64_t* bytes);
+void sop_prepared_free(sop_prepared* p);
+int sop_replicas_admit(sop_engine* e, sop_prepared* const* p, const int64_t* nsteps, int n,
+                       int* replicas, int* admitted);
+/* Final energies (6 per replica), observables (5) and status of each listed
+ * replica, computed in one pass, then the replicas are removed.  Any output
+ * pointer may be NULL. */
+int sop_replicas_retire(sop_engine* e, const int* replicas, int n, double* energy6, double* obs5,
+                        int* status);
 int sop_replica_remove(sop_engine* e, int replica);
 int sop_replica_set_params(sop_engine* e, int replica, const sop_params* p);
 int sop_replica_get_params(sop_engine* e, int replica, sop_params* p);
@@ -202,6 +222,12 @@ int sop_run(sop_engine* e, int64_t nsteps);
  * during the chunk are returned in finished[0..*nfinished) (cap entries). */
 int sop_replica_start(sop_engine* e, int replica, int64_t nsteps);
 int sop_run_chunk(sop_engine* e, int64_t steps, int* finished, int cap, int* nfinished);
+/* sop_run_chunk in two halves: _begin launches the steps and returns; the
+ * host may then do host-only work (sop_prepare) while the GPU runs;
+ * _end waits and hands back the replicas whose window closed.  Between the
+ * two, no other call may use the engine. */
+int sop_run_chunk_begin(sop_engine* e, int64_t steps);
+int sop_run_chunk_end(sop_engine* e, int* finished, int cap, int* nfinished);
 /* End-to-end call with HOST buffers (restart semantics, sop.cpp:132-147):
  * load unc_pos/vel of every active replica (packed in replica-id order,
  * 3*nbead each), evaluate the initial force, run nsteps, write them back. */
@@ -290,6 +316,8 @@ int sop_server_poll(sop_server* s, sop_request_result* out, int cap, int* n);
 /* seconds since the server was created (the clock of submit/start/finish) */
 int sop_server_clock(sop_server* s, double* now_s);
 int sop_server_stats(sop_server* s, int64_t* bead_steps, int* active, int* queued);
+/* Host time the pumps spent admitting, running chunks and retiring (s). */
+int sop_server_timing(sop_server* s, double* admit_s, double* run_s, double* retire_s);
 
 /* ---- synthetic systems (test and bench workloads) -------------------------------- */
 /* Seeded self-avoiding 3.8 A chain compacted by 2000-step-style minimisation. */

@@ -315,6 +315,8 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(dalloc(&e->d_items, cap / 32 + cfg.max_replicas + 16));
   e->items_cap = cap / 32 + cfg.max_replicas + 16;
   CK(cudaMallocHost((void**)&e->h_rep, sizeof(RepDev)));
+  CK(cudaMallocHost((void**)&e->h_reps, sizeof(RepDev) * cfg.max_replicas));
+  CK(cudaMallocHost((void**)&e->h_done, sizeof(int)));
   e->beads.init(cap);
   e->lists.init(lcap);
   e->nats.init(ecap);
@@ -360,6 +362,8 @@ extern "C" int sop_engine_destroy(sop_engine* e) {
                   A.bin_cell, A.cstart, A.ccur, A.bin_hdr, A.step_ctr};
   for (void* p : ptrs) cudaFree(p);
   if (e->h_rep) cudaFreeHost(e->h_rep);
+  if (e->h_reps) cudaFreeHost(e->h_reps);
+  if (e->h_done) cudaFreeHost(e->h_done);
   for (int k = 0; k < 4; k++) if (e->ev[k]) cudaEventDestroy(e->ev[k]);
   cudaStreamDestroy(e->stream);
   delete e;
@@ -609,21 +613,6 @@ static int compute_L(const sop_system_desc* d, const Topo& T, int mode) {
   return (L + 7) / 8 * 8;
 }
 
-extern "C" int sop_system_bytes(const sop_engine* e, const sop_system_desc* d, int64_t* bytes) {
-  if (!e || !d || !bytes || d->nbead <= 0) return SOP_ERR_ARG;
-  Topo T;
-  int rc = build_topology(d, T);
-  if (rc) return rc;
-  long long L = compute_L(d, T, d->params.list_mode);
-  long long n = d->nbead;
-  long long b = n * (2 * 24 + 2 * 32 + 12 + 24 + 24 + 16 + 16 + 8 + 4) + n * L * 4 +
-                n * (16 + 4 + 4) + (cell_capacity((int)n) + 1) * 8 +
-                (long long)T.nat.size() * 16 + (long long)T.bnd.size() * 24 +
-                (long long)T.ang.size() * 4 + (long long)T.exc.size() * 4;
-  *bytes = b;
-  return SOP_OK;
-}
-
 extern "C" int sop_engine_free_bytes(const sop_engine* e, int64_t* bytes) {
   if (!e || !bytes) return SOP_ERR_ARG;
   size_t fr = 0, tot = 0;
@@ -711,8 +700,26 @@ int sop::build_now(sop_engine* e, int r, int mode) {
   return SOP_OK;
 }
 
-extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* replica) {
-  if (!e || !d || !replica || d->nbead <= 0 || !d->xyz) return SOP_ERR_ARG;
+// ---- admission: host preparation, then device placement -------------------------
+
+// A system prepared on the host (topology, row length, byte count): no
+// device work, so it can run while the GPU steps other replicas.
+struct sop_prepared {
+  Topo T;
+  sop_params params{};
+  int n = 0, L = 0;
+  std::vector<double> xyz, vel;
+  int64_t bytes = 0;
+};
+
+static int64_t replica_bytes(long long n, long long L, const Topo& T) {
+  return n * (2 * 24 + 2 * 32 + 12 + 24 + 24 + 24 + 16 + 16 + 8 + 4) + n * L * 4 +
+         n * (16 + 4 + 4) + (cell_capacity((int)n) + 1) * 8 + (long long)T.nat.size() * 16 +
+         (long long)T.bnd.size() * 24 + (long long)T.ang.size() * 4 + (long long)T.exc.size() * 4;
+}
+
+static int prepare(const sop_system_desc* d, sop_prepared& P) {
+  if (!d || d->nbead <= 0 || !d->xyz) return SOP_ERR_ARG;
   if ((d->nbnd && (!d->ib || !d->jb || !d->r0)) || (d->nang && (!d->ia || !d->ka)) ||
       (d->nnat && (!d->in_ || !d->jn || !d->rn)) || (d->nexcl && (!d->ie || !d->je)))
     return SOP_ERR_ARG;
@@ -721,17 +728,62 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
     if (!std::isfinite(d->xyz[q])) return SOP_ERR_ARG;
   RepDev rd;
   std::memset(&rd, 0, sizeof rd);
-  int rc = fill_repdev(d->params, rd);
+  int rc = fill_repdev(d->params, rd);  // validates the parameters
   if (rc) return rc;
-  Topo T;
-  rc = build_topology(d, T);
+  rc = build_topology(d, P.T);
   if (rc) return rc;
+  P.params = d->params;
+  P.n = d->nbead;
+  P.L = compute_L(d, P.T, d->params.list_mode);
+  P.xyz.assign(d->xyz, d->xyz + 3 * (size_t)P.n);
+  if (d->vel) P.vel.assign(d->vel, d->vel + 3 * (size_t)P.n);
+  else P.vel.clear();
+  P.bytes = replica_bytes(P.n, P.L, P.T);
+  return SOP_OK;
+}
+
+// Queue the positions (both buffers and their staged float pairs), the
+// velocities and zero increments of replica r (no synchronization: copies
+// from pageable memory return once the data is staged).
+static int stage_state(sop_engine* e, int r, const double* xyz, const double* vel) {
+  Replica& R = e->reps[r];
+  const int n = R.n;
+  const long long off = R.off, cap = e->cap;
+  std::vector<double> soa(3 * (size_t)n), vs(3 * (size_t)n, 0.0);
+  std::vector<float> zero(3 * (size_t)n, 0.0f);
+  std::vector<float4> st(2 * (size_t)n);
+  for (int i = 0; i < n; i++) {
+    float h[3], l[3];
+    for (int c = 0; c < 3; c++) {
+      soa[(size_t)c * n + i] = xyz[3 * i + c];
+      if (vel) vs[(size_t)c * n + i] = vel[3 * i + c];
+      split_double(xyz[3 * i + c], h[c], l[c]);
+    }
+    // .w: bead type and chain id as integer bits
+    st[2 * i] = make_float4(h[0], h[1], h[2], u2f((uint32_t)R.type[i]));
+    st[2 * i + 1] = make_float4(l[0], l[1], l[2], u2f((uint32_t)R.chain[i]));
+  }
+  for (int b = 0; b < 2; b++) {
+    for (int c = 0; c < 3; c++) CK(h2d(e->A.X[b] + c * cap + off, soa.data() + (size_t)c * n, n, e->stream));
+    CK(h2d(e->A.stage[b] + 2 * off, st.data(), 2 * (size_t)n, e->stream));
+  }
+  for (int c = 0; c < 3; c++) {
+    CK(h2d(e->A.vel + c * cap + off, vs.data() + (size_t)c * n, n, e->stream));
+    CK(h2d(e->A.incr + c * cap + off, zero.data() + (size_t)c * n, n, e->stream));
+  }
+  return SOP_OK;
+}
+
+// Place a prepared system into a free slot: arenas, uploads and the replica
+// descriptor, all queued on the stream without a synchronization.  The
+// caller builds its lists.  SOP_ERR_FULL when a slot or an arena is missing.
+static int place(sop_engine* e, const sop_prepared& P, int* replica) {
+  const Topo& T = P.T;
   int slot = -1;
   for (int k = 0; k < (int)e->reps.size(); k++)
     if (!e->reps[k].live) { slot = k; break; }
   if (slot < 0) return SOP_ERR_FULL;
-  const int n = d->nbead;
-  const int L = compute_L(d, T, d->params.list_mode);
+  const int n = P.n, L = P.L;
   const long long ncell_e = cell_capacity(n) + 1;
   long long off = 0, nlb = 0, nb = 0, bb = 0, ab = 0, xb = 0, cb = 0;
   {
@@ -752,6 +804,16 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
       }
     }
   }
+  if (nb + (long long)T.nat.size() > 0x7fffffffLL) {
+    e->beads.release(off, n);
+    e->lists.release(nlb, (long long)n * L);
+    e->nats.release(nb, (long long)T.nat.size());
+    e->bnds.release(bb, (long long)T.bnd.size());
+    e->angs.release(ab, (long long)T.ang.size());
+    e->excs.release(xb, (long long)T.exc.size());
+    e->cells.release(cb, ncell_e);
+    return SOP_ERR_FULL;
+  }
   Replica& R = e->reps[slot];
   R = Replica();
   R.live = true;
@@ -765,20 +827,23 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
   R.bnd_base = bb; R.nbnd_e = (long long)T.bnd.size();
   R.ang_base = ab; R.nang_e = (long long)T.ang.size();
   R.exc_base = xb; R.nexc_e = (long long)T.exc.size();
-  R.params = d->params;
+  R.params = P.params;
   R.type = T.type;
   R.chain = T.chain;
   R.nnat_pairs = T.nnat_pairs;
-  // rebase the per-bead ranges onto the arenas
+  // the per-bead ranges rebased onto the arenas
+  std::vector<int4> topo(T.topo);
+  std::vector<int2> exc_rng(T.exc_rng);
   for (int i = 0; i < n; i++) {
-    T.topo[i].x += (int)nb;
-    T.topo[i].y += (int)bb;
-    T.topo[i].z += (int)ab;
-    T.exc_rng[i].x += (int)xb;
+    topo[i].x += (int)nb;
+    topo[i].y += (int)bb;
+    topo[i].z += (int)ab;
+    exc_rng[i].x += (int)xb;
   }
-  if (nb + (long long)T.nat.size() > 0x7fffffffLL) return SOP_ERR_FULL;
-  CK(h2d(e->A.topo + off, T.topo.data(), n, e->stream));
-  CK(h2d(e->A.exc_rng + off, T.exc_rng.data(), n, e->stream));
+  // host-to-device copies from pageable memory return once the data is
+  // staged, so the host vectors may go out of scope right after
+  CK(h2d(e->A.topo + off, topo.data(), n, e->stream));
+  CK(h2d(e->A.exc_rng + off, exc_rng.data(), n, e->stream));
   CK(h2d(e->A.nat + nb, T.nat.data(), T.nat.size(), e->stream));
   CK(h2d(e->A.nat_r0 + nb, T.nat_r0.data(), T.nat_r0.size(), e->stream));
   CK(h2d(e->A.bnd + bb, T.bnd.data(), T.bnd.size(), e->stream));
@@ -786,6 +851,9 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
   CK(h2d(e->A.ang + ab, T.ang.data(), T.ang.size(), e->stream));
   CK(h2d(e->A.exc + xb, T.exc.data(), T.exc.size(), e->stream));
   CK(cudaMemsetAsync(e->A.nl_cnt + off, 0, sizeof(int) * n, e->stream));
+  RepDev rd;
+  std::memset(&rd, 0, sizeof rd);
+  fill_repdev(P.params, rd);
   rd.off = (int)off;
   rd.n = n;
   rd.type_mask = 0;
@@ -795,29 +863,122 @@ extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* rep
   rd.nat_base = (int)nb; rd.bnd_base = (int)bb; rd.ang_base = (int)ab; rd.exc_base = (int)xb;
   rd.cell_base = cb;
   rd.cell_cap = (int)cell_capacity(n);
-  int pi = d->params.pull_i, pj = d->params.pull_j;
+  int pi = P.params.pull_i, pj = P.params.pull_j;
   rd.pull_i = (pi >= 0 && pi < n) ? pi : 0;
   rd.pull_j = (pj >= 0 && pj < n) ? pj : n - 1;
   rd.t = 0;
   rd.cur = 0;
   rd.inlup = 1;
   rd.active = 1;
-  rc = put_rep(e, slot, rd);
+  CK(cudaMemcpyAsync(e->A.rep + slot, &rd, sizeof rd, cudaMemcpyHostToDevice, e->stream));
+  int rc = stage_state(e, slot, P.xyz.data(), P.vel.empty() ? nullptr : P.vel.data());
   if (rc) return rc;
-  rc = upload_positions(e, slot, d->xyz, 3);
-  if (rc) return rc;
-  rc = upload_velocities(e, slot, d->vel);
-  if (rc) return rc;
-  // set-up of underdamped_ctrl (sop.cpp:117-125): lists at the initial positions
-  rc = rebuild_fit(e, slot, d->params.list_mode);
-  if (rc) {
-    if (rc == SOP_ERR_FULL) sop_replica_remove(e, slot);
-    return rc;
-  }
   e->layout_dirty = true;
   *replica = slot;
   return SOP_OK;
 }
+
+__global__ void k_begin_many(RepDev* rep, const int* ids, const long long* nsteps, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || nsteps[k] <= 0) return;
+  RepDev* R = &rep[ids[k]];
+  if (!R->active) return;
+  R->t_end = R->t + nsteps[k];
+  R->first_pending = 1;
+  R->running = 1;
+}
+
+extern "C" int sop_prepare(const sop_system_desc* d, sop_prepared** out) {
+  if (!out) return SOP_ERR_ARG;
+  *out = nullptr;
+  std::unique_ptr<sop_prepared> P(new (std::nothrow) sop_prepared());
+  if (!P) return SOP_ERR_NOMEM;
+  int rc = prepare(d, *P);
+  if (rc) return rc;
+  *out = P.release();
+  return SOP_OK;
+}
+
+extern "C" int sop_prepared_bytes(const sop_prepared* p, int64_t* bytes) {
+  if (!p || !bytes) return SOP_ERR_ARG;
+  *bytes = p->bytes;
+  return SOP_OK;
+}
+
+extern "C" void sop_prepared_free(sop_prepared* p) { delete p; }
+
+extern "C" int sop_system_bytes(const sop_engine* e, const sop_system_desc* d, int64_t* bytes) {
+  if (!e || !d || !bytes) return SOP_ERR_ARG;
+  sop_prepared P;
+  int rc = prepare(d, P);
+  if (rc) return rc;
+  *bytes = P.bytes;
+  return SOP_OK;
+}
+
+extern "C" int sop_replicas_admit(sop_engine* e, sop_prepared* const* p, const int64_t* nsteps, int n,
+                                  int* ids, int* admitted) {
+  if (!e || (n > 0 && (!p || !ids)) || !admitted || n < 0) return SOP_ERR_ARG;
+  *admitted = 0;
+  if (n == 0) return SOP_OK;
+  if (e->chunk_open) return SOP_ERR_STATE;
+  CK(cudaSetDevice(e->cfg.device));
+  CK(cudaStreamSynchronize(e->stream));  // the id / step scratch below is reused
+  // 1. places, in order, until a slot or an arena is missing
+  int k = 0;
+  for (; k < n; k++) {
+    if (!p[k]) return SOP_ERR_ARG;
+    const int rc = place(e, *p[k], &ids[k]);
+    if (rc == SOP_ERR_FULL) break;
+    if (rc) {  // nothing of this batch is admitted
+      for (int w = 0; w < k; w++) sop_replica_remove(e, ids[w]);
+      return rc;
+    }
+  }
+  const int m = k;
+  if (m == 0) return SOP_ERR_FULL;
+  // 2. one list build for all of them (sop.cpp:117-125: lists at the initial positions)
+  CK(cudaMemcpyAsync(e->d_pack_ids, ids, m * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  CK(launch_prologue(e->A, e->d_pack_ids, m, nullptr, 1, -1, e->pro_grid, e->stream));
+  e->launches += kPrologueLaunches;
+  CK(cudaMemcpyAsync(e->h_reps, e->A.rep, sizeof(RepDev) * e->cfg.max_replicas,
+                     cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  // 3. rows longer than estimated grow (rare), then the run windows open
+  for (int q = 0; q < m; q++) {
+    if (!(e->h_reps[ids[q]].status & SOP_ST_LIST_OVERFLOW)) continue;
+    int rc = grow_rows(e, ids[q], e->h_reps[ids[q]].max_row);
+    if (rc == SOP_OK) rc = rebuild_fit(e, ids[q], e->reps[ids[q]].params.list_mode);
+    if (rc) {  // no room for its rows: nothing of this batch is admitted
+      for (int w = 0; w < m; w++) sop_replica_remove(e, ids[w]);
+      return rc;
+    }
+  }
+  if (nsteps) {
+    std::vector<long long> ns(nsteps, nsteps + m);
+    CK(cudaMemcpyAsync(e->d_pack_off, ns.data(), m * sizeof(long long), cudaMemcpyHostToDevice,
+                       e->stream));
+    k_begin_many<<<(m + 127) / 128, 128, 0, e->stream>>>(e->A.rep, e->d_pack_ids, e->d_pack_off, m);
+    e->launches++;
+    CK(cudaGetLastError());
+  }
+  *admitted = m;
+  return SOP_OK;
+}
+
+extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* replica) {
+  if (!e || !replica) return SOP_ERR_ARG;
+  sop_prepared P;
+  int rc = prepare(d, P);
+  if (rc) return rc;
+  sop_prepared* pp = &P;
+  int got = 0;
+  rc = sop_replicas_admit(e, &pp, nullptr, 1, replica, &got);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(e->stream));
+  return got == 1 ? SOP_OK : SOP_ERR_FULL;
+}
+
 
 // Move replica r's list rows to a range of row length >= need (+50% and 32
 // spare), releasing the old range; the caller rebuilds.  Clears the overflow
@@ -1224,12 +1385,53 @@ extern "C" int sop_replica_start(sop_engine* e, int r, int64_t nsteps) {
   return SOP_OK;
 }
 
-extern "C" int sop_run_chunk(sop_engine* e, int64_t steps, int* finished, int cap, int* nfinished) {
-  if (!e || steps < 0 || (cap > 0 && !finished)) return SOP_ERR_ARG;
+extern "C" int sop_replicas_retire(sop_engine* e, const int* ids, int n, double* energy6, double* obs5,
+                                   int* status) {
+  if (!e || n < 0 || (n > 0 && !ids)) return SOP_ERR_ARG;
+  if (n == 0) return SOP_OK;
+  for (int k = 0; k < n; k++)
+    if (!live(e, ids[k])) return SOP_ERR_ARG;
+  if (e->chunk_open) return SOP_ERR_STATE;
+  CK(cudaSetDevice(e->cfg.device));
+  CK(cudaStreamSynchronize(e->stream));
+  // final energies and observables of all of them, then one read-back
+  CK(cudaMemcpyAsync(e->d_pack_ids, ids, n * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  CK(launch_energy(e->A, e->d_pack_ids, n, e->stream));
+  CK(launch_observables(e->A, e->d_pack_ids, n, e->stream));
+  e->launches += 2;
+  CK(cudaMemcpyAsync(e->h_reps, e->A.rep, sizeof(RepDev) * e->cfg.max_replicas,
+                     cudaMemcpyDeviceToHost, e->stream));
+  int err = 0;
+  CK(cudaMemcpyAsync(&err, e->A.err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  static const RepDev zero{};
+  for (int k = 0; k < n; k++) {
+    const RepDev& d = e->h_reps[ids[k]];
+    if (energy6) std::memcpy(energy6 + 6 * k, d.energy, sizeof d.energy);
+    if (obs5) std::memcpy(obs5 + 5 * k, d.obs, sizeof d.obs);
+    if (status) status[k] = d.status | (err ? 0x100 : 0);
+    // removal: descriptor cleared (queued), arenas returned
+    CK(cudaMemcpyAsync(e->A.rep + ids[k], &zero, sizeof zero, cudaMemcpyHostToDevice, e->stream));
+    sop::Replica& R = e->reps[ids[k]];
+    e->beads.release(R.off, R.n);
+    e->lists.release(R.nl_base, (long long)R.n * R.L);
+    e->nats.release(R.nat_base, R.nnat_e);
+    e->bnds.release(R.bnd_base, R.nbnd_e);
+    e->angs.release(R.ang_base, R.nang_e);
+    e->excs.release(R.exc_base, R.nexc_e);
+    e->cells.release(R.cell_base, R.ncell_e);
+    R = sop::Replica();
+  }
+  e->layout_dirty = true;
+  return SOP_OK;
+}
+
+extern "C" int sop_run_chunk_begin(sop_engine* e, int64_t steps) {
+  if (!e || steps < 0) return SOP_ERR_ARG;
+  if (e->chunk_open) return SOP_ERR_STATE;
   CK(cudaSetDevice(e->cfg.device));
   int rc = refresh_layout(e);
   if (rc) return rc;
-  if (nfinished) *nfinished = 0;
   if (e->active.empty() || steps == 0) return SOP_OK;
   rc = capture_graph(e);
   if (rc) return rc;
@@ -1245,17 +1447,32 @@ extern "C" int sop_run_chunk(sop_engine* e, int64_t steps, int* finished, int ca
     if (rc) return rc;
   }
   CK(cudaEventRecord(e->ev[1], e->stream));
-  int nd = 0;
-  CK(cudaMemcpyAsync(&nd, e->A.done_cnt, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaMemcpyAsync(e->h_done, e->A.done_cnt, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  e->chunk_open = true;
+  return SOP_OK;
+}
+
+extern "C" int sop_run_chunk_end(sop_engine* e, int* finished, int cap, int* nfinished) {
+  if (!e || (cap > 0 && !finished)) return SOP_ERR_ARG;
+  if (nfinished) *nfinished = 0;
+  if (!e->chunk_open) return SOP_OK;
+  e->chunk_open = false;
   CK(cudaStreamSynchronize(e->stream));
   float ms = 0;
   cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]);
   e->last_total_ms = ms;
-  nd = std::min(nd, e->A.done_cap);
+  const int nd = std::min(*e->h_done, e->A.done_cap);
   if (nd > 0 && cap > 0)
     CK(cudaMemcpy(finished, e->A.done_list, std::min(nd, cap) * sizeof(int), cudaMemcpyDeviceToHost));
   if (nfinished) *nfinished = nd;
   return check_errors(e);
+}
+
+extern "C" int sop_run_chunk(sop_engine* e, int64_t steps, int* finished, int cap, int* nfinished) {
+  if (!e || steps < 0 || (cap > 0 && !finished)) return SOP_ERR_ARG;
+  int rc = sop_run_chunk_begin(e, steps);
+  if (rc) return rc;
+  return sop_run_chunk_end(e, finished, cap, nfinished);
 }
 
 int sop::begin_all(sop_engine* e, int64_t nsteps) {

@@ -59,6 +59,9 @@ struct sop_engine {
   sop::RangeAlloc beads, lists, nats, bnds, angs, excs, cells;
   std::vector<sop::Replica> reps;
   sop::RepDev* h_rep = nullptr;  // pinned staging for descriptor copies
+  sop::RepDev* h_reps = nullptr; // pinned copy of every descriptor (batched admission / retirement)
+  int* h_done = nullptr;         // pinned: replicas whose window closed in the open chunk
+  bool chunk_open = false;       // a chunk was launched and not yet waited for
   // batched layout
   int* d_ids = nullptr;             // active replica ids; scratch slots at the end
   sop::StepItem* d_items = nullptr; // step work items; scratch at the end

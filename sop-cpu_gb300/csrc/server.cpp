@@ -1,14 +1,18 @@
 // Continuous-batching server over the engine's C ABI.
 //
-// Requests (a system + a step count) queue in arrival order.  Each pump:
-//   1. admits queued requests while a slot is free and their device bytes fit
-//      the memory budget and the engine's arenas (head of line waits),
-//   2. opens a run window per admitted request and advances every running
-//      request by one chunk of graph-captured batched steps,
-//   3. retires the requests whose window closed: final energies and
-//      observables are read, the replica is removed, its memory freed.
-// Requests that arrive while others run join at the next pump, so their work
-// overlaps on the device with requests already in flight.  State stays
+// Requests (a system + a step count) queue in arrival order; each is prepared
+// on the host at submission (topology, row sizing, device bytes), outside
+// the server lock.  A pump is pipelined with the device:
+//   1. it waits for the chunk the previous pump launched and retires, in one
+//      batch, the requests whose run window closed in it: final energies,
+//      observables and status are read, the replicas removed, memory freed;
+//   2. it admits, in one batch, queued requests in order while a slot is
+//      free and their device bytes fit the memory budget and the engine's
+//      arenas (head of line waits): one list build, run windows opened;
+//   3. it launches the next chunk of graph-captured batched steps for every
+//      running request and returns while the device runs it.
+// The caller's submissions between pumps therefore overlap device work, and
+// requests that arrive while others run join at the next pump.  State stays
 // resident on the GPU from admission to retirement.
 #include <algorithm>
 #include <chrono>
@@ -23,57 +27,16 @@
 
 namespace {
 
-// A system description that owns copies of its arrays.
-struct OwnedDesc {
-  std::vector<double> xyz, vel, r0, rn;
-  std::vector<int> type, chain, ib, jb, ia, ka, in, jn, ie, je;
-  sop_system_desc d{};
-
-  template <class T>
-  static void copy(std::vector<T>& v, const T* p, long long n) {
-    if (p && n > 0) v.assign(p, p + n);
-    else v.clear();
-  }
-  template <class T>
-  static const T* ptr(const std::vector<T>& v) {
-    return v.empty() ? nullptr : v.data();
-  }
-
-  void assign(const sop_system_desc& s) {
-    const long long n = s.nbead;
-    copy(xyz, s.xyz, 3 * n);
-    copy(vel, s.vel, 3 * n);
-    copy(type, s.bead_type, n);
-    copy(chain, s.chain, n);
-    copy(ib, s.ib, s.nbnd);
-    copy(jb, s.jb, s.nbnd);
-    copy(r0, s.r0, s.nbnd);
-    copy(ia, s.ia, s.nang);
-    copy(ka, s.ka, s.nang);
-    copy(in, s.in_, s.nnat);
-    copy(jn, s.jn, s.nnat);
-    copy(rn, s.rn, s.nnat);
-    copy(ie, s.ie, s.nexcl);
-    copy(je, s.je, s.nexcl);
-    d = s;
-    d.xyz = ptr(xyz);
-    d.vel = ptr(vel);
-    d.bead_type = ptr(type);
-    d.chain = ptr(chain);
-    d.ib = ptr(ib); d.jb = ptr(jb); d.r0 = ptr(r0);
-    d.ia = ptr(ia); d.ka = ptr(ka);
-    d.in_ = ptr(in); d.jn = ptr(jn); d.rn = ptr(rn);
-    d.ie = ptr(ie); d.je = ptr(je);
-  }
-};
-
 struct Request {
   int64_t id = 0;
-  OwnedDesc desc;
+  sop_prepared* prep = nullptr;  // released once admitted
   int64_t nsteps = 0;
   int64_t bytes = 0;
+  int64_t nbead = 0;
   double submit_s = 0, start_s = 0;
   int replica = -1;
+
+  ~Request() { sop_prepared_free(prep); }
 };
 
 }  // namespace
@@ -89,7 +52,13 @@ struct sop_server {
   int64_t next_id = 1;
   int64_t bead_steps = 0;
   int64_t mem_used = 0;
-  std::vector<int> finished;
+  bool chunk_open = false;
+  std::vector<int> finished, ids;
+  std::vector<double> energy, obs;
+  std::vector<int> status;
+  std::vector<sop_prepared*> batch;
+  std::vector<int64_t> batch_steps;
+  double t_admit = 0, t_run = 0, t_retire = 0;  // seconds spent in each pump phase
 
   double now() const {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -108,7 +77,12 @@ extern "C" int sop_server_create(const sop_server_config* cfg, sop_server** out)
     s->cfg.engine.max_replicas = s->cfg.max_active + 8;
   int rc = sop_engine_create(&s->cfg.engine, &s->eng);
   if (rc) return rc;
-  s->finished.resize(s->cfg.engine.max_replicas);
+  const int R = s->cfg.engine.max_replicas;
+  s->finished.resize(R);
+  s->ids.resize(R);
+  s->energy.resize(6 * (size_t)R);
+  s->obs.resize(5 * (size_t)R);
+  s->status.resize(R);
   s->t0 = std::chrono::steady_clock::now();
   *out = s.release();
   return SOP_OK;
@@ -116,7 +90,11 @@ extern "C" int sop_server_create(const sop_server_config* cfg, sop_server** out)
 
 extern "C" int sop_server_destroy(sop_server* s) {
   if (!s) return SOP_ERR_ARG;
-  if (s->eng) sop_engine_destroy(s->eng);
+  if (s->eng) {
+    int nf = 0;
+    if (s->chunk_open) sop_run_chunk_end(s->eng, s->finished.data(), (int)s->finished.size(), &nf);
+    sop_engine_destroy(s->eng);
+  }
   delete s;
   return SOP_OK;
 }
@@ -125,11 +103,12 @@ extern "C" int sop_server_submit(sop_server* s, const sop_system_desc* d, int64_
                                  int64_t* request_id) {
   if (!s || !d || nsteps < 1 || d->nbead < 1 || !d->xyz) return SOP_ERR_ARG;
   std::unique_ptr<Request> r(new Request());
-  r->desc.assign(*d);
-  r->nsteps = nsteps;
-  std::lock_guard<std::mutex> lk(s->mu);
-  int rc = sop_system_bytes(s->eng, &r->desc.d, &r->bytes);
+  int rc = sop_prepare(d, &r->prep);  // host work, no lock held
+  if (rc == SOP_OK) rc = sop_prepared_bytes(r->prep, &r->bytes);
   if (rc) return rc;
+  r->nsteps = nsteps;
+  r->nbead = d->nbead;
+  std::lock_guard<std::mutex> lk(s->mu);
   r->id = s->next_id++;
   r->submit_s = s->now();
   if (request_id) *request_id = r->id;
@@ -137,68 +116,121 @@ extern "C" int sop_server_submit(sop_server* s, const sop_system_desc* d, int64_
   return SOP_OK;
 }
 
-static void fail(sop_server* s, Request& r, int status) {
+static sop_request_result result_of(const Request& r) {
   sop_request_result res{};
   res.request_id = r.id;
-  res.status = status;
-  res.nbead = r.desc.d.nbead;
+  res.nbead = r.nbead;
   res.steps = r.nsteps;
   res.submit_s = r.submit_s;
+  res.start_s = r.start_s;
+  return res;
+}
+
+static void fail(sop_server* s, Request& r, int status) {
+  sop_request_result res = result_of(r);
+  res.status = status;
   res.start_s = res.finish_s = s->now();
   s->done.push_back(res);
+}
+
+// Retire, in one batch, the requests whose replicas are listed.
+static int retire(sop_server* s, const int* reps, int nf) {
+  int n = 0;
+  for (int k = 0; k < nf; k++)
+    if (s->running.count(reps[k])) s->ids[n++] = reps[k];
+  if (n == 0) return SOP_OK;
+  const int rc = sop_replicas_retire(s->eng, s->ids.data(), n, s->energy.data(), s->obs.data(),
+                                     s->status.data());
+  const double t = s->now();
+  for (int k = 0; k < n; k++) {
+    auto it = s->running.find(s->ids[k]);
+    Request& r = *it->second;
+    sop_request_result res = result_of(r);
+    res.status = rc;
+    if (rc == SOP_OK) {
+      res.replica_status = s->status[k];
+      std::memcpy(res.energy, &s->energy[6 * k], sizeof res.energy);
+      std::memcpy(res.observables, &s->obs[5 * k], sizeof res.observables);
+    }
+    res.finish_s = t;
+    s->done.push_back(res);
+    s->bead_steps += r.nbead * r.nsteps;
+    s->mem_used -= r.bytes;
+    s->running.erase(it);
+  }
+  return rc;
+}
+
+// Admit queued requests in order, in batches, until the head of the queue
+// does not fit.  A batch the engine refuses for a reason other than room
+// fails its head request, and admission goes on with the next.
+static int admit(sop_server* s) {
+  while (!s->queue.empty()) {
+    s->batch.clear();
+    s->batch_steps.clear();
+    int64_t mem = s->mem_used;
+    const int slots = s->cfg.max_active - (int)s->running.size();
+    for (size_t k = 0; k < s->queue.size() && (int)s->batch.size() < slots; k++) {
+      const Request& r = *s->queue[k];
+      if (s->cfg.memory_budget > 0 && mem + r.bytes > s->cfg.memory_budget) break;
+      mem += r.bytes;
+      s->batch.push_back(r.prep);
+      s->batch_steps.push_back(r.nsteps);
+    }
+    if (s->batch.empty()) return SOP_OK;
+    int got = 0;
+    const int rc = sop_replicas_admit(s->eng, s->batch.data(), s->batch_steps.data(),
+                                      (int)s->batch.size(), s->ids.data(), &got);
+    if (rc == SOP_ERR_FULL) return SOP_OK;  // wait for retirements to free the arenas
+    if (rc) {
+      fail(s, *s->queue.front(), rc);
+      s->queue.pop_front();
+      continue;
+    }
+    const double t = s->now();
+    for (int k = 0; k < got; k++) {
+      std::unique_ptr<Request> r = std::move(s->queue.front());
+      s->queue.pop_front();
+      sop_prepared_free(r->prep);
+      r->prep = nullptr;
+      r->replica = s->ids[k];
+      r->start_s = t;
+      s->mem_used += r->bytes;
+      s->running[r->replica] = std::move(r);
+    }
+    if (got < (int)s->batch.size()) return SOP_OK;  // the engine is full
+  }
+  return SOP_OK;
 }
 
 extern "C" int sop_server_pump(sop_server* s, int* pending) {
   if (!s) return SOP_ERR_ARG;
   std::lock_guard<std::mutex> lk(s->mu);
-  // 1. admission, in arrival order
-  while (!s->queue.empty() && (int)s->running.size() < s->cfg.max_active) {
-    Request& r = *s->queue.front();
-    if (s->cfg.memory_budget > 0 && s->mem_used + r.bytes > s->cfg.memory_budget) break;
-    int rep = -1;
-    int rc = sop_replica_add(s->eng, &r.desc.d, &rep);
-    if (rc == SOP_ERR_FULL) break;  // wait for retirements to free the arenas
-    if (rc == SOP_OK) rc = sop_replica_start(s->eng, rep, r.nsteps);
-    if (rc) {
-      if (rep >= 0) sop_replica_remove(s->eng, rep);
-      fail(s, r, rc);
-      s->queue.pop_front();
-      continue;
-    }
-    r.replica = rep;
-    r.start_s = s->now();
-    s->mem_used += r.bytes;
-    s->running[rep] = std::move(s->queue.front());
-    s->queue.pop_front();
-  }
-  // 2. one chunk for everything in flight
-  if (!s->running.empty()) {
+  double tp = s->now();
+  // 1. the chunk in flight ends; its finished requests retire
+  if (s->chunk_open) {
     int nf = 0;
-    int rc = sop_run_chunk(s->eng, s->cfg.chunk_steps, s->finished.data(), (int)s->finished.size(), &nf);
+    s->chunk_open = false;
+    int rc = sop_run_chunk_end(s->eng, s->finished.data(), (int)s->finished.size(), &nf);
     if (rc) return rc;
-    // 3. retirement
-    for (int k = 0; k < nf; k++) {
-      const int rep = s->finished[k];
-      auto it = s->running.find(rep);
-      if (it == s->running.end()) continue;
-      Request& r = *it->second;
-      sop_request_result res{};
-      res.request_id = r.id;
-      res.nbead = r.desc.d.nbead;
-      res.steps = r.nsteps;
-      res.submit_s = r.submit_s;
-      res.start_s = r.start_s;
-      int64_t t = 0;
-      res.status = sop_energy_eval(s->eng, rep, res.energy);
-      if (res.status == SOP_OK) res.status = sop_observables(s->eng, rep, res.observables);
-      if (res.status == SOP_OK) res.status = sop_replica_status(s->eng, rep, &res.replica_status, &t);
-      res.finish_s = s->now();
-      s->done.push_back(res);
-      s->bead_steps += (int64_t)r.desc.d.nbead * r.nsteps;
-      s->mem_used -= r.bytes;
-      sop_replica_remove(s->eng, rep);
-      s->running.erase(it);
-    }
+    double tq = s->now();
+    s->t_run += tq - tp;
+    rc = retire(s, s->finished.data(), nf);
+    tp = s->now();
+    s->t_retire += tp - tq;
+    if (rc) return rc;
+  }
+  // 2. admission, in arrival order
+  int rc = admit(s);
+  double tq = s->now();
+  s->t_admit += tq - tp;
+  if (rc) return rc;
+  // 3. the next chunk for everything in flight, left running
+  if (!s->running.empty()) {
+    rc = sop_run_chunk_begin(s->eng, s->cfg.chunk_steps);
+    if (rc) return rc;
+    s->chunk_open = true;
+    s->t_run += s->now() - tq;
   }
   if (pending) *pending = (int)(s->queue.size() + s->running.size());
   return SOP_OK;
@@ -217,6 +249,15 @@ extern "C" int sop_server_poll(sop_server* s, sop_request_result* out, int cap, 
 extern "C" int sop_server_clock(sop_server* s, double* now_s) {
   if (!s || !now_s) return SOP_ERR_ARG;
   *now_s = s->now();
+  return SOP_OK;
+}
+
+extern "C" int sop_server_timing(sop_server* s, double* admit_s, double* run_s, double* retire_s) {
+  if (!s) return SOP_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (admit_s) *admit_s = s->t_admit;
+  if (run_s) *run_s = s->t_run;
+  if (retire_s) *retire_s = s->t_retire;
   return SOP_OK;
 }
 

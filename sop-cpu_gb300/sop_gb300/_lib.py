@@ -129,6 +129,13 @@ _PROTOS = {
     "sop_run": (C.c_int, [VP, C.c_int64]),
     "sop_replica_start": (C.c_int, [VP, C.c_int, C.c_int64]),
     "sop_run_chunk": (C.c_int, [VP, C.c_int64, IP, C.c_int, IP]),
+    "sop_run_chunk_begin": (C.c_int, [VP, C.c_int64]),
+    "sop_run_chunk_end": (C.c_int, [VP, IP, C.c_int, IP]),
+    "sop_prepare": (C.c_int, [C.POINTER(SystemDesc), C.POINTER(VP)]),
+    "sop_prepared_bytes": (C.c_int, [VP, C.POINTER(C.c_int64)]),
+    "sop_prepared_free": (None, [VP]),
+    "sop_replicas_admit": (C.c_int, [VP, C.POINTER(VP), C.POINTER(C.c_int64), C.c_int, IP, IP]),
+    "sop_replicas_retire": (C.c_int, [VP, IP, C.c_int, DP, DP, IP]),
     "sop_run_host": (C.c_int, [VP, DP, DP, C.c_int64, DP, DP]),
     "sop_last_run_timing": (C.c_int, [VP, DP, DP, C.POINTER(C.c_int64)]),
     "sop_profile_steps": (C.c_int, [VP, C.c_int64, DP, DP]),
@@ -146,6 +153,7 @@ _PROTOS = {
     "sop_server_poll": (C.c_int, [VP, C.POINTER(RequestResult), C.c_int, IP]),
     "sop_server_clock": (C.c_int, [VP, DP]),
     "sop_server_stats": (C.c_int, [VP, C.POINTER(C.c_int64), IP, IP]),
+    "sop_server_timing": (C.c_int, [VP, DP, DP, DP]),
     "sop_synth_chain": (C.c_int, [C.c_uint64, C.c_int, C.c_int, DP]),
     "sop_synth_globule": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.c_int, DP]),
     "sop_neighbor_list_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -71,3 +71,9 @@ class Server:
         bs, a, q = C.c_int64(), C.c_int(), C.c_int()
         L.check(L.lib().sop_server_stats(self.h, C.byref(bs), C.byref(a), C.byref(q)), "sop_server_stats")
         return dict(bead_steps=bs.value, active=a.value, queued=q.value)
+
+    def timing(self):
+        """Seconds the pumps spent admitting, running chunks and retiring."""
+        a, r, t = C.c_double(), C.c_double(), C.c_double()
+        L.check(L.lib().sop_server_timing(self.h, C.byref(a), C.byref(r), C.byref(t)), "sop_server_timing")
+        return dict(admit_s=a.value, run_s=r.value, retire_s=t.value)
