@@ -277,9 +277,11 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(dalloc(&A.pairs_out, e->pairs_cap));
   CK(dalloc(&A.pairs_cnt, 1));
   CK(dalloc(&A.err, 1));
-  CK(dalloc(&A.step_ctr, 3));
-  CK(cudaMemsetAsync(A.step_ctr, 0, 3 * sizeof(int), e->stream));
+  // {next item, finished warps, any_rebuild, prologue exits}
+  CK(dalloc(&A.step_ctr, 4));
+  CK(cudaMemsetAsync(A.step_ctr, 0, 4 * sizeof(int), e->stream));
   A.any_rebuild = A.step_ctr + 2;
+  A.pro_exit = A.step_ctr + 3;
   // grouped skin rebuilds: replicas past this fraction of their trigger
   // distance rebuild together with one that must (0 = off)
   A.group_frac2 = cfg.group_rebuild_pct > 0
@@ -1331,6 +1333,7 @@ static int capture_graph(sop_engine* e) {
     int rc = enqueue_batched_step(e);
     if (rc) { cudaStreamEndCapture(e->stream, &g); return rc; }
   }
+  e->graph_launches = e->launches - before;
   e->launches = before;  // counted when replayed
   CK(cudaStreamEndCapture(e->stream, &g));
   CK(cudaGraphInstantiate(&e->graph_exec, g, 0));
@@ -1355,7 +1358,7 @@ int sop::run_batched(sop_engine* e, int64_t nsteps, bool timed) {
   const int64_t full = iters / S;
   for (int64_t k = 0; k < full; k++) {
     CK(cudaGraphLaunch(e->graph_exec, e->stream));
-    e->launches += kStepLaunches * S;
+    e->launches += e->graph_launches;
   }
   for (int64_t k = full * S; k < iters; k++) {
     rc = enqueue_batched_step(e);
@@ -1440,7 +1443,7 @@ extern "C" int sop_run_chunk_begin(sop_engine* e, int64_t steps) {
   const int S = e->cfg.graph_steps;
   for (int64_t k = 0; k < steps / S; k++) {
     CK(cudaGraphLaunch(e->graph_exec, e->stream));
-    e->launches += kStepLaunches * S;
+    e->launches += e->graph_launches;
   }
   for (int64_t k = steps / S * S; k < steps; k++) {
     rc = enqueue_batched_step(e);
@@ -1495,7 +1498,7 @@ int sop::run_steps(sop_engine* e, int64_t steps, float* ms) {
   const int S = e->cfg.graph_steps;
   for (int64_t k = 0; k < steps / S; k++) {
     CK(cudaGraphLaunch(e->graph_exec, e->stream));
-    e->launches += kStepLaunches * S;
+    e->launches += e->graph_launches;
   }
   for (int64_t k = steps / S * S; k < steps; k++) {
     rc = enqueue_batched_step(e);

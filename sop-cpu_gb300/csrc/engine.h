@@ -87,6 +87,7 @@ struct sop_engine {
   int pairs_cap = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int64_t launches = 0;
+  int64_t graph_launches = 0;  // launches of one replay of the step graph
   double last_total_ms = 0, last_step_ms = -1;
   int64_t last_step_launches = 0;
 };

@@ -706,25 +706,43 @@ __device__ int decide_one(const DevArrays& A, int r, int force_build, int build_
 }
 
 // K0 + K1: the step bookkeeping of every listed replica and, for those that
-// rebuild their lists this step, the cell binning; persistent CTAs, one
-// replica at a time (thread 0 decides, the CTA bins).  nrep comes from device
-// memory when nrep_dev is set, so a captured graph keeps working when
-// replicas are admitted or retired.
+// rebuild their lists this step, the cell binning.  CTA b owns the replicas
+// k = b, b + grid, ...: its threads decide them in parallel (one thread per
+// replica), then the CTA bins those that rebuild, one after another.  nrep
+// comes from device memory when nrep_dev is set, so a captured graph keeps
+// working when replicas are admitted or retired.  The last CTA to finish
+// clears the grouped-rebuild signal (every CTA has read it by then).
 __global__ void __launch_bounds__(kBinThreads, 2) k_prologue(DevArrays A, const int* rep_ids,
                                                             const int* nrep_dev, int nrep_host,
                                                             int force_build, int build_mode,
                                                             int dyn_bytes) {
   extern __shared__ __align__(16) int bsm[];
-  __shared__ int s_build;
+  __shared__ int s_build[kBinThreads];
   const int nrep = nrep_dev ? *nrep_dev : nrep_host;
-  const int group = *A.any_rebuild;  // cleared by k_build, after every CTA here read it
-  for (int k = blockIdx.x; k < nrep; k += gridDim.x) {
-    const int r = rep_ids[k];
-    if (threadIdx.x == 0) s_build = decide_one(A, r, force_build, build_mode, group);
+  const int group = *A.any_rebuild;
+  const int mine = nrep > (int)blockIdx.x ? (nrep - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+  for (int m0 = 0; m0 < mine; m0 += (int)blockDim.x) {
+    const int cnt = min(mine - m0, (int)blockDim.x);
+    if ((int)threadIdx.x < cnt) {
+      const int r = rep_ids[blockIdx.x + (m0 + threadIdx.x) * gridDim.x];
+      s_build[threadIdx.x] = decide_one(A, r, force_build, build_mode, group);
+    }
     __syncthreads();
-    const int b = s_build;
-    if (b >= 0) bin_replica(A, r, b >> 8, b & 0xFF, bsm, dyn_bytes / 4);
+    for (int q = 0; q < cnt; q++) {
+      const int b = s_build[q];
+      if (b < 0) continue;
+      bin_replica(A, rep_ids[blockIdx.x + (m0 + q) * gridDim.x], b >> 8, b & 0xFF, bsm, dyn_bytes / 4);
+      __syncthreads();
+    }
     __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(A.pro_exit, 1) == (int)gridDim.x - 1) {
+      __threadfence();
+      *A.pro_exit = 0;
+      if (!force_build) *A.any_rebuild = 0;
+    }
   }
 }
 
@@ -739,8 +757,6 @@ __global__ void __launch_bounds__(kBuildThreads, 2) k_build(DevArrays A, int dyn
   double* red = reinterpret_cast<double*>(dyn);
   const int cnt = min(*A.unit_cnt, A.unit_cap);
   const int sb = A.slice_beads;
-  // the grouped-rebuild signal of the last step has been read by k_prologue
-  if (blockIdx.x == 0 && threadIdx.x == 0) *A.any_rebuild = 0;
   for (int u = blockIdx.x; u < cnt; u += gridDim.x) {
     const int4 w = A.units[u];
     const int r = w.x, kind = w.y & 0xFF, mode = w.y >> 8;

@@ -49,6 +49,7 @@ struct DevArrays {
   int slice_beads;    // beads per list-build slice unit
   int* step_ctr;      // warp-task step kernel: {next item, finished warps}
   int* any_rebuild;   // a SKIN displacement trigger fired in the last step
+  int* pro_exit;      // k_prologue CTAs finished (the last one closes the step's bookkeeping)
   float group_frac2;  // (grouping fraction of the trigger distance)^2; > 1 = no grouping
 };
 

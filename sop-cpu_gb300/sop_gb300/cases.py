@@ -3,6 +3,7 @@ single-kernel captures).  Run as
 
     PYTHONPATH=sop-cpu_gb300 python -m sop_gb300.cases mix --steps 3
     PYTHONPATH=sop-cpu_gb300 python -m sop_gb300.cases build --steps 4
+    PYTHONPATH=sop-cpu_gb300 python -m sop_gb300.cases mixbuild --steps 3
     PYTHONPATH=sop-cpu_gb300 python -m sop_gb300.cases globule --steps 3
 
 mix      512 replicas, N log-uniform 30-1500 (seed 2000), T 0.4-0.9, skin lists
@@ -10,6 +11,9 @@ mix      512 replicas, N log-uniform 30-1500 (seed 2000), T 0.4-0.9, skin lists
          per --steps.
 build    one 1500-bead chain, neighbor list rebuilt before every step (nnlup 1):
          every prologue is a full list build.
+mixbuild the mix with the reference's neighbor-list cadence at nnlup 1: every
+         replica rebuilds its lists before every step (the load of a grouped
+         skin rebuild of the whole batch).
 globule  100 chains x 500 beads in one compact globule (50,000 beads), skin
          lists: the large single-system workload.
 
@@ -29,14 +33,18 @@ WORKLOAD_SCRIPT = [("set", "zeta", "50"), ("set", "t_step", "0.05"), ("set", "te
                    ("set", "boxl", "2000"), ("set", "ncell", "250"), ("set", "run", "1")]
 
 
-def mix_engine(count=512, lo=30, hi=1500, skin=2.0, **cfg):
+def mix_engine(count=512, lo=30, hi=1500, skin=2.0, every_step=False, **cfg):
     systems, temps = S.mixed_batch(count, lo, hi, seed=2000)
     nb = sum(s.nbead for s in systems)
     eng = Engine(0, max_beads=max(1 << 16, int(nb * 1.3)), max_replicas=count + 16,
                  max_list_entries=int(nb * 200), **cfg)
+    script = [c if c[1] != "nnlup" else ("set", "nnlup", "1") for c in WORKLOAD_SCRIPT]
     for k, (s, T) in enumerate(zip(systems, temps)):
-        eng.add(s, make_params(WORKLOAD_SCRIPT, T=float(T), seed=77_000 + k,
-                               list_mode="skin", skin=skin))
+        if every_step:
+            p = make_params(script, T=float(T), seed=77_000 + k)
+        else:
+            p = make_params(WORKLOAD_SCRIPT, T=float(T), seed=77_000 + k, list_mode="skin", skin=skin)
+        eng.add(s, p)
     return eng, systems
 
 
@@ -58,13 +66,14 @@ def globule_engine(nchain=100, chain_len=500, skin=2.0):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("case", choices=("mix", "build", "globule"))
+    ap.add_argument("case", choices=("mix", "mixbuild", "build", "globule"))
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warm", type=int, default=10, help="batched steps before the profiled ones")
     ap.add_argument("--tune", type=int, default=0,
                     help="autotune with this many steps per trial before profiling")
     a = ap.parse_args(argv)
-    eng, systems = {"mix": mix_engine, "build": build_engine, "globule": globule_engine}[a.case]()
+    eng, systems = {"mix": mix_engine, "mixbuild": lambda: mix_engine(every_step=True),
+                    "build": build_engine, "globule": globule_engine}[a.case]()
     if a.warm:
         eng.run(a.warm)
     if a.tune:
