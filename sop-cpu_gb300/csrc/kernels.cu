@@ -157,12 +157,10 @@ __device__ __forceinline__ void fence_async_smem() {
 // K2: neighbor/pair-list enumeration of a slice of beads (k_build units)
 
 constexpr int kWarpNat = 64;       // native partners per bead staged per warp
-constexpr int kStencilSlots = 128; // (2K+1)^3 <= 125 stencil cells, 4 per lane
 
 struct BuildSmem {
   int wnat[kBuildThreads / 32][kWarpNat];
-  int wbeg[kBuildThreads / 32][kStencilSlots];
-  int wpre[kBuildThreads / 32][kStencilSlots];
+  int wseg[kBuildThreads / 32][32];
   int s_maxrow, s_status;
 };
 
@@ -284,6 +282,16 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
       h.ncell = h.nx * h.ny * h.nz;
       h.ok = !(h.status & SOP_ST_GRID);
     }
+    // the replica's cutoffs, once per binning instead of once per listed bead
+    for (int a = 0; a < kMaxTypes; a++)
+      for (int b = 0; b < 2; b++) {
+        const int ta = a ? a : 1, tb = b + 1;
+        const double rl = 2.5 * c_ff.sigma_rep[ta][tb] + (double)R->skin;
+        h.rl2d[a][b] = (mode == SOP_LIST_SKIN) ? rl * rl : c_ff.rc2_nl[ta][tb];
+        h.pl2d[a][b] = c_ff.rc2_pl[ta][tb];  // (2.5 sigma)^2, sop.cpp:539-541
+        h.rl2f[a][b] = (float)h.rl2d[a][b];
+        h.pl2f[a][b] = (float)h.pl2d[a][b];
+      }
     H = h;
   }
   __syncthreads();
@@ -407,16 +415,15 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
 __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0, int b1,
                             BuildSmem& B, unsigned char* dyn, int dyn_bytes) {
   RepDev* R = &A.rep[r];
-  const BinHdr H = A.bin_hdr[r];
-  if (!H.ok) return;  // the binning recorded why
+  const BinHdr* H = A.bin_hdr + r;
+  if (!H->ok) return;  // the binning recorded why
   const int n = R->n, off = R->off, tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5;
-  const int nx = H.nx, ny = H.ny, nz = H.nz, ncell = H.ncell, K = H.K, SK = 2 * K + 1;
+  const int nx = H->nx, ny = H->ny, nz = H->nz, ncell = H->ncell, K = H->K, SK = 2 * K + 1;
   const int ncs = SK * SK * SK;
   const float4* S = A.stage[src] + 2 * (long long)off;
   const double* X = A.X[src];
   const long long cap = A.cap;
-  const float skin = R->skin;
 
   const float4* P = A.bin_p + off;
   const int* sorted = A.bin_sorted + off;
@@ -441,11 +448,10 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
 
   const long long nl_base = R->nl_base;
   const int L = R->L;
-  const float margin = H.margin;
+  const float margin = H->margin;
   int my_status = 0, my_max = 0;
   int* wnat = B.wnat[warp];
-  int* wbeg = B.wbeg[warp];  // first sorted slot of each stencil cell
-  int* wpre = B.wpre[warp];  // exclusive prefix of the stencil-cell counts
+  int* wseg = B.wseg[warp];  // per window position: sorted slot - candidate index of its cell
   const unsigned lt_mask = (1u << lane) - 1u;
   const int nwarp = nt >> 5;
   // this lane's stencil cells 4 lane + q as packed offsets (dx+K | dy+K << 4 |
@@ -471,14 +477,9 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
     if (nat_in_smem)
       for (int k = lane; k < nat_cnt; k += 32) wnat[k] = A.nat[tp.x + k].x & (int)kIdx;
     __syncwarp();
-    // list and pair cutoffs^2 against partner types 1 and 2 (type 0 reads as 1)
-    const int tA = ti ? ti : 1;
-    const double rlA = 2.5 * c_ff.sigma_rep[tA][1] + (double)skin,
-                 rlB = 2.5 * c_ff.sigma_rep[tA][2] + (double)skin;
-    const double rl2d1 = (mode == SOP_LIST_SKIN) ? rlA * rlA : c_ff.rc2_nl[tA][1];
-    const double rl2d2 = (mode == SOP_LIST_SKIN) ? rlB * rlB : c_ff.rc2_nl[tA][2];
-    const double pl2d1 = c_ff.rc2_pl[tA][1], pl2d2 = c_ff.rc2_pl[tA][2];  // (2.5 sigma)^2, sop.cpp:539-541
-    const float rl2f1 = (float)rl2d1, rl2f2 = (float)rl2d2, pl2f1 = (float)pl2d1, pl2f2 = (float)pl2d2;
+    // list and pair cutoffs^2 against partner types 1 and 2
+    const float rl2f1 = H->rl2f[ti][0], rl2f2 = H->rl2f[ti][1];
+    const float pl2f1 = H->pl2f[ti][0], pl2f2 = H->pl2f[ti][1];
     // the stencil cells (dz, dy, dx from -K to K) flattened into one candidate
     // range: lane l owns stencil cells 4l..4l+3, a warp scan gives offsets
     int cnt4[4], beg4[4], lsum = 0;
@@ -503,30 +504,37 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
       if (lane >= o) incl += y;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    {
-      int pre = incl - lsum;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        wbeg[4 * lane + q] = beg4[q];
-        wpre[4 * lane + q] = pre;
-        pre += cnt4[q];
-      }
-    }
-    __syncwarp();
-    int cnt = 0;  // warp-uniform
+    const int pre0 = incl - lsum;  // candidate index of this lane's first cell
+    int carry = 0;  // sorted slot - candidate index of the cell running into the window
+    int cnt = 0;    // warp-uniform
     for (int base = 0; base < total; base += 32) {
+      // every non-empty cell that starts inside the window marks its first
+      // position; a lane's cell is the last mark at or before it
+      unsigned bits = 0;
+      {
+        int pre = pre0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int at = pre - base;
+          if (cnt4[q] > 0 && at >= 0 && at < 32) {
+            bits |= 1u << at;
+            wseg[at] = beg4[q] - pre;
+          }
+          pre += cnt4[q];
+        }
+      }
+      const unsigned marks = __reduce_or_sync(0xffffffffu, bits);
+      __syncwarp();
+      const unsigned upto = marks & (0xffffffffu >> (31 - lane));
+      const int segoff = upto ? wseg[31 - __clz(upto)] : carry;
+      if (marks) carry = wseg[31 - __clz(marks)];
+      __syncwarp();
       const int f = base + lane;
       bool pass = f < total;
       int j = 0, tj = 1;
       float d2 = 0.f;
       if (pass) {
-        int lo = 0, hi = ncs - 1;  // last stencil cell whose prefix <= f
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (wpre[mid] <= f) lo = mid;
-          else hi = mid - 1;
-        }
-        j = sorted[wbeg[lo] + (f - wpre[lo])];
+        j = sorted[segoff + f];
         const float4 pj = P[j];
         const int code_j = __float_as_int(pj.w), chj = code_j >> 2;
         tj = code_j & 3;
@@ -537,10 +545,10 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
       const long long gj = off + j;
       if (pass && mode != SOP_LIST_NONE && mode != SOP_LIST_CELL) {
         // cell adjacency is the whole predicate in cell mode (cell_list.cpp:86-88)
-        const double rl2 = tj == 2 ? rl2d2 : rl2d1;
         const float rl2f = tj == 2 ? rl2f2 : rl2f1;
         pass = d2 <= rl2f * (1.0f + margin) &&
-               within(d2, rl2f, margin, [&] { return exact_d2(X, cap, gi, gj) < rl2; });
+               within(d2, rl2f, margin,
+                      [&] { return exact_d2(X, cap, gi, gj) < H->rl2d[ti][tj == 2]; });
       }
       if (pass) {  // natives are listed separately (sorted by partner)
         int lo = 0, hi = nat_cnt;
@@ -558,9 +566,8 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
         if (mode == SOP_LIST_NONE) {
           inp = true;  // no pair-list filter without a cutoff type
         } else {
-          const double rc2 = tj == 2 ? pl2d2 : pl2d1;
           inp = within(d2, tj == 2 ? pl2f2 : pl2f1, margin,
-                       [&] { return exact_d2(X, cap, gi, gj) < rc2; });
+                       [&] { return exact_d2(X, cap, gi, gj) < H->pl2d[ti][tj == 2]; });
         }
       }
       const unsigned m = __ballot_sync(0xffffffffu, pass);
@@ -583,12 +590,14 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
       float4 pj = P[j];
       float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
       float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
-      double r0 = A.nat_r0[tp.x + k];
+      const float r0sq = __int_as_float(e.y);  // r0^2 rounded to FP32: the screen's cutoffs
       const long long gj = off + j;
       bool nlb, plb;
       if (mode == SOP_LIST_NEIGHBOR) {
-        double rc = 3.2 * r0, rc2 = rc * rc;  // neighbor_list.cpp:44-47
-        nlb = within(d2, (float)rc2, margin, [&] { return exact_d2(X, cap, gi, gj) < rc2; });
+        nlb = within(d2, 10.24f * r0sq, margin, [&] {
+          const double rc = 3.2 * A.nat_r0[tp.x + k];  // neighbor_list.cpp:44-47
+          return exact_d2(X, cap, gi, gj) < rc * rc;
+        });
       } else if (mode == SOP_LIST_CELL) {
         int c2 = cell[j];
         int jx = c2 % nx, jy = (c2 / nx) % ny, jz = c2 / (nx * ny);
@@ -599,8 +608,10 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
       if (mode == SOP_LIST_NONE) {
         plb = true;
       } else if (nlb) {
-        double rc = 2.5 * r0, rc2 = rc * rc;  // sop.cpp:504-506
-        plb = within(d2, (float)rc2, margin, [&] { return exact_d2(X, cap, gi, gj) < rc2; });
+        plb = within(d2, 6.25f * r0sq, margin, [&] {
+          const double rc = 2.5 * A.nat_r0[tp.x + k];  // sop.cpp:504-506
+          return exact_d2(X, cap, gi, gj) < rc * rc;
+        });
       } else {
         plb = false;
       }
@@ -1053,7 +1064,9 @@ __global__ void __launch_bounds__(256, MB) k_step(DevArrays A, const StepItem* i
   __syncthreads();
   uint32_t parity = 0;
   // a contiguous block of items per CTA; consecutive items of one replica
-  // merge into one bead range, staged once, with no barrier inside it
+  // merge into one bead range, staged once, with no barrier inside it.  (A
+  // CTA's time is set by its chain of items, each with a fixed staging and
+  // row-latency cost, so equal item counts balance better than equal beads.)
   const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
   const int it_end = min(nitems, ((int)blockIdx.x + 1) * per);
   for (int it = (int)blockIdx.x * per; it < it_end;) {

@@ -58,6 +58,10 @@ struct BinHdr {
   int ok, status, nx, ny, nz, K, ncell;  // K: stencil half-width in cells
   float edge, ox, oy, oz, margin;        // margin: relative FP32 screening band
   int cx0, cy0, cz0;                     // cell-mode origin cell (floor(x / lcell))
+  // non-native list and pair cutoffs^2 by [bead type][partner type 1, 2], in
+  // FP64 for the exact decisions and rounded to FP32 for the screen
+  float rl2f[kMaxTypes][2], pl2f[kMaxTypes][2];
+  double rl2d[kMaxTypes][2], pl2d[kMaxTypes][2];
 };
 
 constexpr int kSliceBeads = 32;       // default beads per list-build work unit
