@@ -901,32 +901,42 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
         if (plb != ((e.x & (int)kPL) != 0)) A.nat[tp.x + k].x = e.x ^ (int)kPL;
       }
     }
-    // non-native repulsion (energy.cpp:313-350)
+    // non-native repulsion (energy.cpp:313-350).  Rows start 32-byte aligned
+    // and hold a multiple of 8 entries, so a lane reads four entries with one
+    // 16-byte load (never past the row) and has four partners in flight
     const int cnt = A.nl_cnt[g];
     const long long row = C.nl_base + (long long)i * C.L;
-    for (int k = lane; k < cnt; k += G) {
-      const int e = A.nl[row + k];
-      const int j = e & (int)kIdx;
-      const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
-      const float dx = (hj.x - hi.x) + (lj.x - lo.x);
-      const float dy = (hj.y - hi.y) + (lj.y - lo.y);
-      const float dz = (hj.z - hi.z) + (lj.z - lo.z);
-      const float d2 = dx * dx + dy * dy + dz * dz;
-      const int tj = (int)f2u(hj.w);
-      const float s2 = c_ff.s2[ti][tj];
-      if (e & (int)kPL) {
-        if (d2 >= s2 * (float)kTol) {
-          const float inv = __fdividef(1.0f, d2);
-          const float s = s2 * inv, s3 = s * s * s;
-          const float co = c_ff.fcr[ti][tj] * inv * (2.0f * s3 * s3 + s3);
-          add(co * dx, co * dy, co * dz);
+    const int4* row4 = reinterpret_cast<const int4*>(A.nl + row);
+    for (int q = lane; 4 * q < cnt; q += G) {
+      const int4 e4 = row4[q];
+      const int ev[4] = {e4.x, e4.y, e4.z, e4.w};
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int k = 4 * q + u;
+        if (k >= cnt) break;
+        const int e = ev[u];
+        const int j = e & (int)kIdx;
+        const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
+        const float dx = (hj.x - hi.x) + (lj.x - lo.x);
+        const float dy = (hj.y - hi.y) + (lj.y - lo.y);
+        const float dz = (hj.z - hi.z) + (lj.z - lo.z);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const int tj = (int)f2u(hj.w);
+        const float s2 = c_ff.s2[ti][tj];
+        if (e & (int)kPL) {
+          if (d2 >= s2 * (float)kTol) {
+            const float inv = __fdividef(1.0f, d2);
+            const float s = s2 * inv, s3 = s * s * s;
+            const float co = c_ff.fcr[ti][tj] * inv * (2.0f * s3 * s3 + s3);
+            add(co * dx, co * dy, co * dz);
+          }
         }
-      }
-      if (upd) {
-        const bool plb = within(d2, c_ff.rc2_pl_f[ti][tj], margin, [&] {
-          return exact_d2(Xc, cap, g, (long long)C.off + j) < c_ff.rc2_pl[ti][tj];
-        });
-        if (plb != ((e & (int)kPL) != 0)) A.nl[row + k] = e ^ (int)kPL;
+        if (upd) {
+          const bool plb = within(d2, c_ff.rc2_pl_f[ti][tj], margin, [&] {
+            return exact_d2(Xc, cap, g, (long long)C.off + j) < c_ff.rc2_pl[ti][tj];
+          });
+          if (plb != ((e & (int)kPL) != 0)) A.nl[row + k] = e ^ (int)kPL;
+        }
       }
     }
   }
