@@ -851,7 +851,19 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   const float4 hi = ldp<ST>(S, 2 * i), lo = ldp<ST>(S, 2 * i + 1);
   const int ti = (int)f2u(hi.w);
   const int4 tp = A.topo[g];
+  // the non-native row: rows start 32-byte aligned and hold a multiple of 8
+  // entries, so a lane reads four entries with one 16-byte load (never past
+  // the row); the lane's first quad is in flight during the natives
+  const int cnt = A.nl_cnt[g];
+  const long long row = C.nl_base + (long long)i * C.L;
+  const int4* row4 = reinterpret_cast<const int4*>(A.nl + row);
+  int4 e4n = make_int4(0, 0, 0, 0);
+  if (4 * lane < C.L) e4n = row4[lane];
   const int nat_cnt = tp.w & 0xFFFF, bnd_cnt = (tp.w >> 16) & 0xFF, ang_cnt = (tp.w >> 24) & 0xFF;
+  int4 bn = make_int4(0, 0, 0, 0);
+  int an = 0;
+  if (lane < bnd_cnt) bn = A.bnd[tp.y + lane];
+  if (lane < ang_cnt) an = A.ang[tp.z + lane];
   const bool upd = (C.phase == PH_FIRST || C.phase == PH_NORMAL) && C.mode != SOP_LIST_NONE;
   const double* Xc = A.X[C.cur];
   const float margin = kScreenMargin;
@@ -872,8 +884,11 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
     // native 12-6 attraction (energy.cpp:274-311).  The force vanishes at the
     // native distance, so (r0/d)^12 - (r0/d)^6 is formed from r0^2 - d^2 in
     // two-float arithmetic: with u = r0^2/d^2 - 1, s^3 - 1 = u (u^2 + 3u + 3).
+    int4 en = make_int4(0, 0, 0, 0);  // the lane's next native record, loaded one entry ahead
+    if (lane < nat_cnt) en = A.nat[tp.x + lane];
     for (int k = lane; k < nat_cnt; k += G) {
-      const int4 e = A.nat[tp.x + k];
+      const int4 e = en;
+      if (k + G < nat_cnt) en = A.nat[tp.x + k + G];
       const int j = e.x & (int)kIdx;
       const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
       const float r0sq = __int_as_float(e.y);
@@ -901,14 +916,11 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
         if (plb != ((e.x & (int)kPL) != 0)) A.nat[tp.x + k].x = e.x ^ (int)kPL;
       }
     }
-    // non-native repulsion (energy.cpp:313-350).  Rows start 32-byte aligned
-    // and hold a multiple of 8 entries, so a lane reads four entries with one
-    // 16-byte load (never past the row) and has four partners in flight
-    const int cnt = A.nl_cnt[g];
-    const long long row = C.nl_base + (long long)i * C.L;
-    const int4* row4 = reinterpret_cast<const int4*>(A.nl + row);
+    // non-native repulsion (energy.cpp:313-350), four entries per load, the
+    // next quad loaded while this one is evaluated
     for (int q = lane; 4 * q < cnt; q += G) {
-      const int4 e4 = row4[q];
+      const int4 e4 = e4n;
+      if (4 * (q + G) < cnt) e4n = row4[q + G];
       const int ev[4] = {e4.x, e4.y, e4.z, e4.w};
 #pragma unroll
       for (int u = 0; u < 4; u++) {
@@ -944,7 +956,8 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
     // FENE (energy.cpp:402-447); d^2 - r0^2 in two-float arithmetic so the
     // stretch dev = (d^2 - r0^2)/(d + r0) keeps FP32 relative accuracy.
     for (int k = lane; k < bnd_cnt; k += G) {
-      const int4 b = A.bnd[tp.y + k];
+      const int4 b = bn;
+      if (k + G < bnd_cnt) bn = A.bnd[tp.y + k + G];
       const int j = b.x;
       const float r0 = __int_as_float(b.y), r0h = __int_as_float(b.z), r0l = __int_as_float(b.w);
       const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
@@ -961,7 +974,8 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   if (C.terms & SOP_TERM_ANGLE) {
     // i,i+2 soft-sphere repulsion (energy.cpp:354-400)
     for (int k = lane; k < ang_cnt; k += G) {
-      const int j = A.ang[tp.z + k];
+      const int j = an;
+      if (k + G < ang_cnt) an = A.ang[tp.z + k + G];
       const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
       const float dx = (hj.x - hi.x) + (lj.x - lo.x);
       const float dy = (hj.y - hi.y) + (lj.y - lo.y);
