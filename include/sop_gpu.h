@@ -125,11 +125,12 @@ typedef struct sop_engine_config {
   int graph_steps;       /* steps captured per CUDA graph launch (0 = 20)      */
   int stage_limit;       /* largest replica (beads) whose positions the step
                             kernel stages in shared memory by TMA; larger ones
-                            are gathered through L1 (0 = 2048, <0 = never)    */
+                            are gathered through L1 (0 = 1664, <0 = never)    */
   int chunk_beads;       /* beads per step-kernel work item (0 = 128)          */
   int build_slice_beads; /* beads per list-build work unit, >= 16 (0 = 32)     */
-  int step_min_blocks;   /* step-kernel variant: registers sized for 2 or 3
-                            resident CTAs per SM (0 = 3)                      */
+  int step_min_blocks;   /* step-kernel variant: registers sized for 2, 3 or 4
+                            resident CTAs per SM (0 = 4; 4 needs a stage
+                            limit <= ~1700 to fit, CTA items only)            */
   int step_strategy;     /* 0: CTA work items staged in shared memory; 1: warp
                             tasks gathering through L1/L2 (same results)      */
   int group_rebuild_pct; /* skin-mode replicas whose displacement passed this %

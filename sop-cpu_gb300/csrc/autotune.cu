@@ -116,7 +116,7 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
   // candidates
   const int stage_max = std::min<int>(kStageMax, ((int)e->prop.sharedMemPerBlockOptin - 1024) / 32);
   std::vector<int> stages;
-  for (int s : {-1, 1024, 2048, 4096})
+  for (int s : {-1, 1024, 1664, 2048, 4096})
     if (s <= stage_max) stages.push_back(s);
   struct Knob {
     const char* name;
@@ -129,7 +129,7 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
       {"chunk", &LaunchShape::chunk, {64, 128, 256, 512}},
       {"threads", &LaunchShape::threads, {64, 128, 256}},
       {"lanes", &LaunchShape::lanes, {1, 2, 4}},
-      {"occ", &LaunchShape::min_blocks, {2, 3}},
+      {"occ", &LaunchShape::min_blocks, {2, 3, 4}},
       {"slice", &LaunchShape::slice, {16, 32, 64, 128}},
       {"group", &LaunchShape::group_pct, {0, 30, 50, 70}},
   };

@@ -190,10 +190,10 @@ extern "C" void sop_engine_config_default(sop_engine_config* c) {
   c->block_threads = 256;
   c->lanes_per_bead = 2;
   c->graph_steps = 20;
-  c->stage_limit = 2048;
+  c->stage_limit = 1664;  // 52 KB of staging: four step CTAs per SM
   c->chunk_beads = 128;
   c->build_slice_beads = kSliceBeads;
-  c->step_min_blocks = 3;
+  c->step_min_blocks = 4;
   c->group_rebuild_pct = 50;
 }
 
@@ -226,7 +226,8 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   }
   if (cfg.group_rebuild_pct < 0 || cfg.group_rebuild_pct >= 100) cfg.group_rebuild_pct = 0;
   if (cfg.step_strategy != 1) cfg.step_strategy = 0;
-  if (cfg.step_min_blocks != 2) cfg.step_min_blocks = 3;
+  if (cfg.step_min_blocks < 2 || cfg.step_min_blocks > 4) cfg.step_min_blocks = 3;
+  if (cfg.step_strategy == 1 && cfg.step_min_blocks == 4) cfg.step_min_blocks = 3;
   if (cfg.stage_limit > kStageMax) cfg.stage_limit = kStageMax;
   if (cfg.chunk_beads < 32) cfg.chunk_beads = 32;
   if (cfg.build_slice_beads < kMinSliceBeads) cfg.build_slice_beads = kMinSliceBeads;
@@ -1528,7 +1529,8 @@ sop::LaunchShape sop::get_launch_shape(const sop_engine* e) {
 void sop::set_launch_shape(sop_engine* e, const LaunchShape& s) {
   e->cfg.block_threads = s.threads;
   e->cfg.step_strategy = s.strategy == 1 ? 1 : 0;
-  e->cfg.step_min_blocks = s.min_blocks == 2 ? 2 : 3;
+  e->cfg.step_min_blocks = (s.min_blocks >= 2 && s.min_blocks <= 4) ? s.min_blocks : 3;
+  if (e->cfg.step_strategy == 1 && e->cfg.step_min_blocks == 4) e->cfg.step_min_blocks = 3;
   e->cfg.lanes_per_bead = s.lanes;
   e->cfg.build_slice_beads = std::max(s.slice, kMinSliceBeads);
   e->A.slice_beads = e->cfg.build_slice_beads;

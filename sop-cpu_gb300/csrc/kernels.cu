@@ -1624,11 +1624,14 @@ __global__ void k_export(DevArrays A, int r, int off, int n, int which, int capa
 using StepKernel = void (*)(DevArrays, const StepItem*, const int*, int);
 
 // The step kernel for a strategy (0: CTA items with shared-memory staging,
-// 1: warp tasks), lane count (1, 2, 4, 8, 16) and occupancy target (2, 3).
+// 1: warp tasks), lane count (1, 2, 4, 8, 16) and occupancy target (2, 3,
+// or 4 for CTA items: 64 registers, and 4 CTAs fit an SM when the stage
+// limit is at most ~1700 beads).
 template <int G>
 static StepKernel step_kernel_g(int strategy, int min_blocks) {
   const bool two = min_blocks == 2;
   if (strategy == 1) return two ? k_step_w<G, 2> : k_step_w<G, 3>;
+  if (min_blocks == 4) return k_step<G, 4>;
   return two ? k_step<G, 2> : k_step<G, 3>;
 }
 static StepKernel step_kernel(int lanes, int min_blocks, int strategy) {
@@ -1663,7 +1666,7 @@ cudaError_t init_kernels(int optin_bytes, int sm_bytes) {
   if ((e = optin(k_build, half, &g_build_dyn)) != cudaSuccess) return e;
   if ((e = optin(k_prologue, half, &g_bin_dyn)) != cudaSuccess) return e;
   for (int lanes : {1, 2, 4, 8, 16})
-    for (int mb : {2, 3})
+    for (int mb : {2, 3, 4})
       if ((e = optin(step_kernel(lanes, mb, 0), optin_bytes)) != cudaSuccess) return e;
   return cudaSuccess;
 }
