@@ -15,7 +15,10 @@ e2e        the same metric through sop_run_host: every step uploads all
 plain      the plain one-system-per-launch GPU path (no graph, no batching)
            over the same mix, for the batched/plain ratio.
 roofline   the fused step kernel: algorithmic bytes per launch over its
-           CUDA-event duration against MEASURED_PEAKS.json hbm_gbs.
+           CUDA-event duration against MEASURED_PEAKS.json hbm_gbs; traffic
+           = DRAM bytes per launch of the same kernel on the same workload
+           from the ncu capture summarized in profiles/k_step_mix512.md
+           (caches flushed before the captured pass).
 cpu_baseline  the CPU oracle (the reference algorithm restated in C) on a
            stratified sample of the replicas, all host threads.
 
@@ -101,6 +104,24 @@ def build_workload(args, rank):
     from sop_gb300 import systems as S
     systems, temps = S.mixed_batch(args.replicas, args.lo, args.hi, seed=2000 + 100000 * rank)
     return systems, temps
+
+
+def default_workload(args):
+    """The workload of the recorded capture: 512 chains, N 30-1500, seed 2000."""
+    return (args.replicas, args.lo, args.hi) == (512, 30, 1500) and args.list_mode == "skin"
+
+
+def read_traffic():
+    """DRAM bytes per k_step launch (read + write) recorded from one ncu
+    capture of the default workload, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "k_step_mix512.md")) as f:
+            for line in f:
+                if line.startswith("traffic:"):
+                    return int(line.split()[1])
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
 
 
 def read_peaks():
@@ -464,7 +485,9 @@ def run_gb300(args):
         "large_system": large,
         "force_rel_err": ferr,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": read_traffic() if default_workload(args) else None,
+                     "traffic_note": "ncu, caches flushed before the captured pass",
                      "kernel": "k_step (fused force + Langevin)", "kernel_ms": step_ms,
                      "prologue_ms": pro_ms, "algorithmic_bytes_per_launch": algo},
         "clocks": clk.summary(),
