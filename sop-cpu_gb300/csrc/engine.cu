@@ -278,11 +278,10 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(dalloc(&A.pairs_out, e->pairs_cap));
   CK(dalloc(&A.pairs_cnt, 1));
   CK(dalloc(&A.err, 1));
-  // {next item, finished warps, any_rebuild, prologue exits}
-  CK(dalloc(&A.step_ctr, 4));
-  CK(cudaMemsetAsync(A.step_ctr, 0, 4 * sizeof(int), e->stream));
+  // {next item, finished warps, any_rebuild}
+  CK(dalloc(&A.step_ctr, 3));
+  CK(cudaMemsetAsync(A.step_ctr, 0, 3 * sizeof(int), e->stream));
   A.any_rebuild = A.step_ctr + 2;
-  A.pro_exit = A.step_ctr + 3;
   // grouped skin rebuilds: replicas past this fraction of their trigger
   // distance rebuild together with one that must (0 = off)
   A.group_frac2 = cfg.group_rebuild_pct > 0
@@ -295,10 +294,14 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   // plus an energy and an observables unit
   A.unit_cap = (int)std::min<long long>(cap / kMinSliceBeads + 3LL * cfg.max_replicas + 64, 1LL << 30);
   CK(dalloc(&A.units, A.unit_cap));
-  CK(dalloc(&A.unit_cnt, 2));
+  CK(cudaMemsetAsync(A.units, 0xFF, sizeof(int4) * A.unit_cap, e->stream));  // every slot free (x = -1)
+  // {queued, exited, next ticket, producers done}
+  CK(dalloc(&A.unit_cnt, 4));
   A.unit_exit = A.unit_cnt + 1;
+  A.unit_take = A.unit_cnt + 2;
+  A.pro_done = A.unit_cnt + 3;
   CK(dalloc(&A.slice_done, cfg.max_replicas));
-  CK(cudaMemsetAsync(A.unit_cnt, 0, 2 * sizeof(int), e->stream));
+  CK(cudaMemsetAsync(A.unit_cnt, 0, 4 * sizeof(int), e->stream));
   A.done_cap = cfg.max_replicas;
   CK(dalloc(&A.done_list, A.done_cap));
   CK(dalloc(&A.done_cnt, 1));
@@ -344,7 +347,7 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   e->step_grid = step_blocks_per_sm(cfg.lanes_per_bead, cfg.step_min_blocks, cfg.step_strategy, cfg.block_threads,
                                     e->max_staged) *
                  e->prop.multiProcessorCount;
-  e->pro_grid = 2 * e->prop.multiProcessorCount;  // k_build CTAs over the unit queue
+  e->pro_grid = 2 * e->prop.multiProcessorCount;  // k_prep CTAs (two per SM, all resident)
   for (int k = 0; k < 4; k++) CK(cudaEventCreate(&e->ev[k]));
   CK(cudaStreamSynchronize(e->stream));
   *out = e.release();
@@ -1243,7 +1246,7 @@ int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem*
   return SOP_OK;
 }
 
-// One batched step: k_prologue (bookkeeping, binning), k_build (list slices, energies, observables),
+// One batched step: k_prep (bookkeeping, binning, list slices, energies, observables),
 // k_step, sized by the engine's fixed grids and the device-resident counts.
 int sop::enqueue_batched_step(sop_engine* e) {
   CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0,
@@ -1573,7 +1576,7 @@ extern "C" int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms) {
   k_begin<<<(nrep + 127) / 128, 128, 0, e->stream>>>(e->A.rep, e->d_ids, nrep, nsteps);
   e->launches++;
   const int64_t iters = nsteps + 1;
-  constexpr int kE = 5;  // event marks: start, before k_prologue, after it, after k_build, after k_step
+  constexpr int kE = 5;  // event marks: start, before k_prep, after it, (the same), after k_step
   std::vector<cudaEvent_t> ev(kE * iters);
   for (auto& x : ev) CK(cudaEventCreate(&x));
   for (int64_t s = 0; s < iters; s++) {

@@ -1,16 +1,16 @@
 // GB300 kernels of the SOP hot path.
 //
-//   k_prologue  K0 per-replica step bookkeeping (phase, noise counter, the
-//               reference's nnlup cadence or the displacement trigger) that
-//               queues the step's due work units, and K1 the cell binning of
-//               every replica whose lists are rebuilt this step (one CTA per
-//               replica: shared-memory counting sort into global bins, bead
-//               order within a cell).
-//   k_build     persistent CTAs over those units: K2 neighbor/pair-list
-//               enumeration in slices of beads over the binned stencil, one
-//               warp per bead, cutoffs decided bit-exactly against the
-//               reference's FP64 arithmetic; output-step energies and
-//               observables.
+//   k_prep      one cooperative launch per step: K0 per-replica step
+//               bookkeeping (phase, noise counter, the reference's nnlup
+//               cadence or the displacement trigger) that publishes the
+//               step's due work units, K1 the cell binning of every replica
+//               whose lists are rebuilt this step (one CTA per replica:
+//               shared-memory counting sort into global bins, bead order
+//               within a cell), and, in the same CTAs as consumers, K2
+//               neighbor/pair-list enumeration in slices of beads over the
+//               binned stencil (one warp per bead, cutoffs decided bit-exactly
+//               against the reference's FP64 arithmetic), output-step
+//               energies and observables.
 //   k_step      K3+K4 fused: pair/bond/angle forces in FP32 from positions
 //               staged in shared memory by TMA bulk copies, lane partials to
 //               int64 fixed point and reduced with warp shuffles, counter-
@@ -153,8 +153,8 @@ __device__ __forceinline__ void fence_async_smem() {
 }
 
 // ---------------------------------------------------------------------------------
-// K1: cell binning of one replica by one CTA into global memory (k_prologue)
-// K2: neighbor/pair-list enumeration of a slice of beads (k_build units)
+// K1: cell binning of one replica by one CTA into global memory
+// K2: neighbor/pair-list enumeration of a slice of beads (build units)
 
 constexpr int kWarpNat = 64;       // native partners per bead staged per warp
 
@@ -631,21 +631,32 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
 __device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* red);
 __device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red);
 
-// Work units queued by k_prologue for k_build: {replica, kind | mode << 8, slice, buffer}.
+// Work units of a step's preparation: {replica, kind | mode << 8, slice,
+// buffer}.  A slot becomes valid when its replica id (x >= 0) is stored after
+// the other fields and a fence; the consumer resets x to -1.
 enum UnitKind : int { U_OBS = 1, U_BUILD = 2, U_ENERGY = 3 };
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void publish_unit(int4* slot, int r, int kind_mode, int slice, int buf) {
+  slot->y = kind_mode;
+  slot->z = slice;
+  slot->w = buf;
+  __threadfence();
+  atomicExch(&slot->x, r);
+}
 
 __device__ __forceinline__ void push_units(const DevArrays& A, int r, int kind, int mode, int nsl,
                                            int buf) {
   const int base = atomicAdd(A.unit_cnt, nsl);
   for (int s = 0; s < nsl; s++)
-    if (base + s < A.unit_cap) A.units[base + s] = make_int4(r, kind | (mode << 8), s, buf);
-}
-
-// A list build's slices for k_build (its binning is done by k_prologue).
-__device__ __forceinline__ void push_build(const DevArrays& A, int r, int mode, int n, int buf) {
-  A.slice_done[r] = 0;
-  A.rep[r].max_row = 0;
-  push_units(A, r, U_BUILD, mode, (n + A.slice_beads - 1) / A.slice_beads, buf);
+    if (base + s < A.unit_cap) publish_unit(&A.units[base + s], r, kind | (mode << 8), s, buf);
 }
 
 // Per-replica step bookkeeping, one thread per replica: phase, noise counter,
@@ -655,7 +666,8 @@ __device__ __forceinline__ void push_build(const DevArrays& A, int r, int mode, 
 //   the list build from X_{t-1} in slices (sop.cpp:156-170: rebuild before the step),
 //   the energies of this output step at X_t with pair list PL_t (after the build,
 //   before the step kernel rewrites the pair-list bits).
-// Returns -1, or the build due now as mode | buffer << 8.
+// Returns -1, or the build due now as mode | buffer << 8 (its counters reset;
+// the caller bins the replica, then publishes the build's slices).
 // group: some replica's displacement trigger fired in the last step.
 __device__ int decide_one(const DevArrays& A, int r, int force_build, int build_mode, int group) {
   RepDev* R = &A.rep[r];
@@ -663,7 +675,8 @@ __device__ int decide_one(const DevArrays& A, int r, int force_build, int build_
   if (force_build) {  // build_mode < 0: the replica's own list mode
     const int mode = build_mode >= 0 ? build_mode : Q.mode;
     R->en_after = 0;
-    push_build(A, r, mode, Q.n, Q.cur);
+    A.slice_done[r] = 0;
+    R->max_row = 0;
     return mode | (Q.cur << 8);
   }
   if (Q.obs_pending) {
@@ -711,26 +724,77 @@ __device__ int decide_one(const DevArrays& A, int r, int force_build, int build_
   R->out = out;
   if (out) R->obs_pending = 1;
   R->en_after = need && out;
-  if (need) push_build(A, r, Q.mode, Q.n, prev);
+  if (need) {
+    A.slice_done[r] = 0;
+    R->max_row = 0;
+  }
   if (out && !need) push_units(A, r, U_ENERGY, 0, 1, Q.cur);
   return need ? (Q.mode | (prev << 8)) : -1;
 }
 
-// K0 + K1: the step bookkeeping of every listed replica and, for those that
-// rebuild their lists this step, the cell binning.  CTA b owns the replicas
-// k = b, b + grid, ...: its threads decide them in parallel (one thread per
-// replica), then the CTA bins those that rebuild, one after another.  nrep
-// comes from device memory when nrep_dev is set, so a captured graph keeps
-// working when replicas are admitted or retired.  The last CTA to finish
-// clears the grouped-rebuild signal (every CTA has read it by then).
-__global__ void __launch_bounds__(kBinThreads, 2) k_prologue(DevArrays A, const int* rep_ids,
-                                                            const int* nrep_dev, int nrep_host,
-                                                            int force_build, int build_mode,
-                                                            int dyn_bytes) {
-  extern __shared__ __align__(16) int bsm[];
-  __shared__ int s_build[kBinThreads];
+// One unit: observables, energies, or a list-build slice.  The CTA that
+// finishes the last slice of a build closes it (counters, displacement flag)
+// and, on an output step, computes the energies with the new pair list.
+__device__ void run_unit(const DevArrays& A, int4 w, BuildSmem& B, unsigned char* dyn, int dyn_bytes,
+                         int* s_last) {
+  double* red = reinterpret_cast<double*>(dyn);
+  const int r = w.x, kind = w.y & 0xFF, mode = w.y >> 8;
+  RepDev* R = &A.rep[r];
+  if (kind == U_OBS) {
+    replica_obs(A, R, w.w, red);
+  } else if (kind == U_ENERGY) {
+    replica_energy(A, R, w.w, red);
+  } else if (kind == U_BUILD) {
+    const int sb = A.slice_beads;
+    const int n = R->n, nsl = (n + sb - 1) / sb;
+    const int b0 = w.z * sb, b1 = min(n, b0 + sb);
+    build_slice(A, r, w.w, mode, b0, b1, B, dyn, dyn_bytes);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      *s_last = atomicAdd(&A.slice_done[r], 1) == nsl - 1;
+    }
+    __syncthreads();
+    if (*s_last) {
+      __threadfence();
+      if (threadIdx.x == 0) {
+        R->builds += 1;
+        R->rebuild = 0;
+        R->near = 0;
+      }
+      if (R->en_after) replica_energy(A, R, R->cur, red);
+    }
+  }
+}
+
+constexpr unsigned long long kQueueWaitNs = 2000000000ULL;  // 2 s: never expected
+
+// K0 + K1 + K2 of a step in one cooperative launch (every CTA resident).
+// Producers: CTA b owns the replicas k = b, b + grid, ...; its threads do
+// their bookkeeping in parallel (one thread per replica, observables and
+// energy units published at once), then the CTA bins, one after another, the
+// replicas that rebuild and publishes each one's build slices.  Consumers:
+// every CTA, once its own replicas are done, takes units in ticket order
+// until all producers have finished and the queue is drained, so builds start
+// while other replicas are still being binned.  nrep comes from device memory
+// when nrep_dev is set, so a captured graph keeps working when replicas are
+// admitted or retired.  The last CTA out resets the queue and clears the
+// grouped-rebuild signal (every CTA has read it by then).
+__global__ void __launch_bounds__(kBuildThreads, 2) k_prep(DevArrays A, const int* rep_ids,
+                                                          const int* nrep_dev, int nrep_host,
+                                                          int force_build, int build_mode,
+                                                          int dyn_bytes) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  __shared__ BuildSmem B;
+  __shared__ int s_build[kBuildThreads];
+  __shared__ int s_base, s_last;
+  __shared__ int4 s_unit;
+  int* const bsm = reinterpret_cast<int*>(dyn);
   const int nrep = nrep_dev ? *nrep_dev : nrep_host;
   const int group = *A.any_rebuild;
+  const int sb = A.slice_beads;
+
+  // A. producers
   const int mine = nrep > (int)blockIdx.x ? (nrep - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
   for (int m0 = 0; m0 < mine; m0 += (int)blockDim.x) {
     const int cnt = min(mine - m0, (int)blockDim.x);
@@ -742,67 +806,68 @@ __global__ void __launch_bounds__(kBinThreads, 2) k_prologue(DevArrays A, const 
     for (int q = 0; q < cnt; q++) {
       const int b = s_build[q];
       if (b < 0) continue;
-      bin_replica(A, rep_ids[blockIdx.x + (m0 + q) * gridDim.x], b >> 8, b & 0xFF, bsm, dyn_bytes / 4);
+      const int r = rep_ids[blockIdx.x + (m0 + q) * gridDim.x];
+      bin_replica(A, r, b >> 8, b & 0xFF, bsm, dyn_bytes / 4);
+      // the bins (written by the whole CTA) before the slices that read them
+      __threadfence();
+      __syncthreads();
+      const int nsl = (A.rep[r].n + sb - 1) / sb;
+      if (threadIdx.x == 0) s_base = atomicAdd(A.unit_cnt, nsl);
+      __syncthreads();
+      for (int s = threadIdx.x; s < nsl; s += blockDim.x)
+        if (s_base + s < A.unit_cap)
+          publish_unit(&A.units[s_base + s], r, U_BUILD | ((b & 0xFF) << 8), s, b >> 8);
       __syncthreads();
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(A.pro_exit, 1) == (int)gridDim.x - 1) {
-      __threadfence();
-      *A.pro_exit = 0;
-      if (!force_build) *A.any_rebuild = 0;
-    }
-  }
-}
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd(A.pro_done, 1);
 
-// Persistent CTAs over the unit queue.  The CTA that finishes the last slice
-// of a build closes it (counters, displacement flag) and, on an output step,
-// computes the energies with the new pair list.  The last CTA to exit resets
-// the queue for the next step.
-__global__ void __launch_bounds__(kBuildThreads, 2) k_build(DevArrays A, int dyn_bytes) {
-  extern __shared__ __align__(16) unsigned char dyn[];
-  __shared__ BuildSmem B;
-  __shared__ int s_last;
-  double* red = reinterpret_cast<double*>(dyn);
-  const int cnt = min(*A.unit_cnt, A.unit_cap);
-  const int sb = A.slice_beads;
-  for (int u = blockIdx.x; u < cnt; u += gridDim.x) {
-    const int4 w = A.units[u];
-    const int r = w.x, kind = w.y & 0xFF, mode = w.y >> 8;
-    RepDev* R = &A.rep[r];
-    if (kind == U_OBS) {
-      replica_obs(A, R, w.w, red);
-    } else if (kind == U_ENERGY) {
-      replica_energy(A, R, w.w, red);
-    } else if (kind == U_BUILD) {
-      const int n = R->n, nsl = (n + sb - 1) / sb;
-      const int b0 = w.z * sb, b1 = min(n, b0 + sb);
-      build_slice(A, r, w.w, mode, b0, b1, B, dyn, dyn_bytes);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        __threadfence();
-        s_last = atomicAdd(&A.slice_done[r], 1) == nsl - 1;
-      }
-      __syncthreads();
-      if (s_last) {
-        __threadfence();
-        if (threadIdx.x == 0) {
-          R->builds += 1;
-          R->rebuild = 0;
-          R->near = 0;
+  // B. consumers
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int t = atomicAdd(A.unit_take, 1);
+      int4 w = make_int4(-1, 0, 0, 0);
+      const unsigned long long t0 = globaltimer_ns();
+      for (;;) {
+        if (t < min(ld_volatile(A.unit_cnt), A.unit_cap)) {
+          const int x = ld_volatile(&A.units[t].x);
+          if (x >= 0) {
+            __threadfence();
+            w = make_int4(x, ld_volatile(&A.units[t].y), ld_volatile(&A.units[t].z),
+                          ld_volatile(&A.units[t].w));
+            A.units[t].x = -1;  // free for the next step
+            break;
+          }
+        } else if (ld_volatile(A.pro_done) == (int)gridDim.x) {
+          __threadfence();
+          if (t >= min(ld_volatile(A.unit_cnt), A.unit_cap)) break;  // drained
+          continue;
         }
-        if (R->en_after) replica_energy(A, R, R->cur, red);
+        if (globaltimer_ns() - t0 > kQueueWaitNs) {  // never expected: record and stop
+          atomicOr(A.err, 2);
+          break;
+        }
       }
+      s_unit = w;
     }
+    __syncthreads();
+    const int4 w = s_unit;
+    if (w.x < 0) break;
+    run_unit(A, w, B, dyn, dyn_bytes, &s_last);
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     __threadfence();
     if (atomicAdd(A.unit_exit, 1) == (int)gridDim.x - 1) {
+      __threadfence();
       *A.unit_cnt = 0;
+      *A.unit_take = 0;
+      *A.pro_done = 0;
       *A.unit_exit = 0;
+      if (!force_build) *A.any_rebuild = 0;
     }
   }
 }
@@ -1644,8 +1709,7 @@ static StepKernel step_kernel(int lanes, int min_blocks, int strategy) {
   }
 }
 
-static int g_build_dyn = 48 * 1024;  // k_build dynamic shared memory (set by init_kernels)
-static int g_bin_dyn = 48 * 1024;    // k_prologue dynamic shared memory
+static int g_prep_dyn = 48 * 1024;  // k_prep dynamic shared memory (set by init_kernels)
 
 // Opt a kernel into up to `optin_bytes` of dynamic shared memory per block
 // (less its static shared memory and the per-block reservation).
@@ -1663,8 +1727,7 @@ cudaError_t init_kernels(int optin_bytes, int sm_bytes) {
   cudaError_t e;
   // the prologue kernels run two CTAs per SM: half the SM's shared memory each
   const int half = std::min(optin_bytes, sm_bytes / 2);
-  if ((e = optin(k_build, half, &g_build_dyn)) != cudaSuccess) return e;
-  if ((e = optin(k_prologue, half, &g_bin_dyn)) != cudaSuccess) return e;
+  if ((e = optin(k_prep, half, &g_prep_dyn)) != cudaSuccess) return e;
   for (int lanes : {1, 2, 4, 8, 16})
     for (int mb : {2, 3, 4})
       if ((e = optin(step_kernel(lanes, mb, 0), optin_bytes)) != cudaSuccess) return e;
@@ -1678,14 +1741,22 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, co
   cudaError_t e;
   if (after_decide && (e = cudaEventRecord(after_decide, s)) != cudaSuccess) return e;
   if (grid <= 0) grid = 1;
-  k_prologue<<<grid, kBinThreads, g_bin_dyn, s>>>(A, rep_ids, nrep_dev, nrep, force_build, build_mode,
-                                                  g_bin_dyn);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // cooperative: the consumers wait for every producer CTA, so all must be resident
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kBuildThreads);
+  cfg.dynamicSmemBytes = (size_t)g_prep_dyn;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if ((e = cudaLaunchKernelEx(&cfg, k_prep, A, rep_ids, nrep_dev, nrep, force_build, build_mode,
+                              g_prep_dyn)) != cudaSuccess)
+    return e;
   if (after_bin && (e = cudaEventRecord(after_bin, s)) != cudaSuccess) return e;
-  // the energy / observables units use the same memory as a reduction buffer
-  const int dyn = g_build_dyn;
-  k_build<<<grid, kBuildThreads, dyn, s>>>(A, dyn);
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,

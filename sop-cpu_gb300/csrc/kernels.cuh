@@ -33,13 +33,15 @@ struct DevArrays {
   int* err;           // engine-wide error word (bounded waits that gave up)
   int4* units;        // per-step work queue (builds in slices, energies, observables)
   int* unit_cnt;      // units queued this step
-  int* unit_exit;     // k_build CTAs finished (the last one resets the queue)
+  int* unit_exit;     // k_prep CTAs finished (the last one resets the queue)
+  int* unit_take;     // next unit ticket
+  int* pro_done;      // k_prep CTAs done publishing
   int* slice_done;    // per replica: build slices finished this step
   int unit_cap;
   int* done_list;     // replicas whose run window closed (final step taken)
   int* done_cnt;
   int done_cap;
-  // cell bins of the last list build (k_bin -> k_build)
+  // cell bins of the last list build (binning -> build slices)
   float4* bin_p;      // per bead: position relative to the grid origin, .w = type | chain << 2 (int bits)
   int* bin_sorted;    // per bead slot: local bead ids sorted by cell, bead order within a cell
   int* bin_cell;      // per bead: cell index
@@ -49,7 +51,6 @@ struct DevArrays {
   int slice_beads;    // beads per list-build slice unit
   int* step_ctr;      // warp-task step kernel: {next item, finished warps}
   int* any_rebuild;   // a SKIN displacement trigger fired in the last step
-  int* pro_exit;      // k_prologue CTAs finished (the last one closes the step's bookkeeping)
   float group_frac2;  // (grouping fraction of the trigger distance)^2; > 1 = no grouping
 };
 
@@ -76,10 +77,9 @@ struct StepItem {
 
 constexpr int kStageMax = 6144;       // beads staged in shared memory (192 KB)
 constexpr int kBuildThreads = 512;
-constexpr int kBinThreads = 512;
-// kernel launches of one step: k_prologue (bookkeeping + binning), k_build, k_step
-constexpr int kPrologueLaunches = 2;
-constexpr int kStepLaunches = 3;
+// kernel launches of one step: k_prep (bookkeeping, binning, list builds), k_step
+constexpr int kPrologueLaunches = 1;
+constexpr int kStepLaunches = 2;
 // cells a replica's binning may use (grid cells grow wider beyond that)
 inline long long cell_capacity(int n) { return 4LL * n + 4096; }
 
@@ -88,14 +88,14 @@ void upload_tables(const FFTables& t, cudaStream_t s);
 // at most, sm_bytes per SM.
 cudaError_t init_kernels(int optin_bytes, int sm_bytes);
 
-// Prologue + list build over `nrep` replica ids: k_prologue (bookkeeping, and
-// cell binning of the replicas that rebuild), k_build (persistent CTAs over
-// list slices, energies, observables).
+// Prologue + list build over `nrep` replica ids in one cooperative launch of
+// k_prep (bookkeeping, cell binning of the replicas that rebuild, list slices,
+// energies, observables).
 // force_build: build for every listed replica from the CURRENT buffer
 // (reference-named list updates), else the step cadence decides.
 // nrep / nitems: host counts (grid sizing); *_dev: the same counts in device
 // memory, read by the kernels when given (graphs survive layout changes).
-// after_decide / after_bin: events recorded before and after k_prologue (profiling)
+// after_decide / after_bin: events recorded before and after k_prep (profiling)
 cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, const int* nrep_dev,
                             int force_build, int build_mode, int grid, cudaStream_t s,
                             cudaEvent_t after_decide = nullptr, cudaEvent_t after_bin = nullptr);
