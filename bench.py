@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--lo", type=int, default=30)
     ap.add_argument("--hi", type=int, default=1500)
     ap.add_argument("--list-mode", default="skin", choices=["neighborlist", "skin"])
-    ap.add_argument("--skin", type=float, default=2.0)
+    ap.add_argument("--skin", type=float, default=3.0)
     ap.add_argument("--plain-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--serve-seconds", type=float, default=20.0)
