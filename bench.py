@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--md-steps", type=int, default=500)
-    ap.add_argument("--autotune", type=int, default=40,
+    ap.add_argument("--autotune", type=int, default=150,
                     help="steps per autotuner trial during warm-up (0 = off)")
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--lo", type=int, default=30)
