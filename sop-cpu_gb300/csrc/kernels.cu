@@ -908,161 +908,151 @@ __device__ __forceinline__ float4 ldp(const float4* S, int k) {
   return __ldg(S + k);
 }
 
-template <int G, bool ST>
-__device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, const float4* S,
-                                          int i, int lane, unsigned gmask) {
-  const long long g = (long long)C.off + i;
-  const long long cap = A.cap;
-  const float4 hi = ldp<ST>(S, 2 * i), lo = ldp<ST>(S, 2 * i + 1);
-  const int ti = (int)f2u(hi.w);
-  const int4 tp = A.topo[g];
-  // the non-native row: rows start 32-byte aligned and hold a multiple of 8
-  // entries, so a lane reads four entries with one 16-byte load (never past
-  // the row); the lane's first quad is in flight during the natives
-  const int cnt = A.nl_cnt[g];
-  const long long row = C.nl_base + (long long)i * C.L;
-  const int4* row4 = reinterpret_cast<const int4*>(A.nl + row);
-  int4 e4n = make_int4(0, 0, 0, 0);
-  if (4 * lane < C.L) e4n = row4[lane];
-  const int nat_cnt = tp.w & 0xFFFF, bnd_cnt = (tp.w >> 16) & 0xFF, ang_cnt = (tp.w >> 24) & 0xFF;
-  int4 bn = make_int4(0, 0, 0, 0);
-  int an = 0;
-  if (lane < bnd_cnt) bn = A.bnd[tp.y + lane];
-  if (lane < ang_cnt) an = A.ang[tp.z + lane];
-  const bool upd = (C.phase == PH_FIRST || C.phase == PH_NORMAL) && C.mode != SOP_LIST_NONE;
-  const double* Xc = A.X[C.cur];
-  const float margin = kScreenMargin;
-  // every pair / bond / angle contribution is added in int64 fixed point, so
-  // the force is an exact integer sum: independent of list order, of lane
-  // count and of when the lists were built
-  long long Fx = 0, Fy = 0, Fz = 0;
-  float mag = 0.f;  // sum of |contributions| of this lane: bounds the int64 sums, carries NaN/inf
+// Exact force accumulator of one bead (a lane's or a thread's share): every
+// pair / bond / angle contribution is added in int64 fixed point, so the force
+// is an exact integer sum, independent of list order, of how the entries are
+// split among lanes or threads and of when the lists were built.
+struct FixAcc {
+  long long x = 0, y = 0, z = 0;
+  float mag = 0.f;  // sum of |contributions|: bounds the int64 sums, carries NaN/inf
   int st = 0;
-  auto add = [&](float cx, float cy, float cz) {
-    Fx += fixed_from_float(cx);
-    Fy += fixed_from_float(cy);
-    Fz += fixed_from_float(cz);
+  __device__ __forceinline__ void add(float cx, float cy, float cz) {
+    x += fixed_from_float(cx);
+    y += fixed_from_float(cy);
+    z += fixed_from_float(cz);
     mag += fabsf(cx) + fabsf(cy) + fabsf(cz);
-  };
+  }
+  // NaN, inf or a share out of the fixed-point range
+  __device__ __forceinline__ int range_status() const { return mag <= kFixMax ? 0 : SOP_ST_NONFINITE; }
+};
 
-  if (C.terms & SOP_TERM_VDW) {
-    // native 12-6 attraction (energy.cpp:274-311).  The force vanishes at the
-    // native distance, so (r0/d)^12 - (r0/d)^6 is formed from r0^2 - d^2 in
-    // two-float arithmetic: with u = r0^2/d^2 - 1, s^3 - 1 = u (u^2 + 3u + 3).
-    int4 en = make_int4(0, 0, 0, 0);  // the lane's next native record, loaded one entry ahead
-    if (lane < nat_cnt) en = A.nat[tp.x + lane];
-    for (int k = lane; k < nat_cnt; k += G) {
-      const int4 e = en;
-      if (k + G < nat_cnt) en = A.nat[tp.x + k + G];
-      const int j = e.x & (int)kIdx;
-      const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
-      const float r0sq = __int_as_float(e.y);
-      float dx, dy, dz, d2;
-      const float diff = d2_minus(hi, lo, hj, lj, r0sq, __int_as_float(e.z), dx, dy, dz, d2);
-      if (e.x & (int)kPL) {
-        if (d2 >= (float)kTol * r0sq) {
-          const int tj = (int)f2u(hj.w);
-          const float inv = __fdividef(1.0f, d2);
-          const float u = -diff * inv;                 // s - 1, s = r0^2/d^2
-          const float s3m1 = u * fmaf(u, u + 3.0f, 3.0f);  // s^3 - 1
-          const float s3 = 1.0f + s3m1;
-          const float co = c_ff.fca[ti][tj] * inv * (s3 * s3m1);
-          add(co * dx, co * dy, co * dz);
-        }
-      }
-      if (upd) {
-        bool plb = false;
-        if (e.x & (int)kNL) {
-          plb = within(d2, 6.25f * r0sq, margin, [&] {
-            double rc = 2.5 * A.nat_r0[tp.x + k], rc2 = rc * rc;
-            return exact_d2(Xc, cap, g, (long long)C.off + j) < rc2;
-          });
-        }
-        if (plb != ((e.x & (int)kPL) != 0)) A.nat[tp.x + k].x = e.x ^ (int)kPL;
-      }
-    }
-    // non-native repulsion (energy.cpp:313-350), four entries per load, the
-    // next quad loaded while this one is evaluated
-    for (int q = lane; 4 * q < cnt; q += G) {
-      const int4 e4 = e4n;
-      if (4 * (q + G) < cnt) e4n = row4[q + G];
-      const int ev[4] = {e4.x, e4.y, e4.z, e4.w};
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int k = 4 * q + u;
-        if (k >= cnt) break;
-        const int e = ev[u];
-        const int j = e & (int)kIdx;
-        const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
-        const float dx = (hj.x - hi.x) + (lj.x - lo.x);
-        const float dy = (hj.y - hi.y) + (lj.y - lo.y);
-        const float dz = (hj.z - hi.z) + (lj.z - lo.z);
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        const int tj = (int)f2u(hj.w);
-        const float s2 = c_ff.s2[ti][tj];
-        if (e & (int)kPL) {
-          if (d2 >= s2 * (float)kTol) {
-            const float inv = __fdividef(1.0f, d2);
-            const float s = s2 * inv, s3 = s * s * s;
-            const float co = c_ff.fcr[ti][tj] * inv * (2.0f * s3 * s3 + s3);
-            add(co * dx, co * dy, co * dz);
-          }
-        }
-        if (upd) {
-          const bool plb = within(d2, c_ff.rc2_pl_f[ti][tj], margin, [&] {
-            return exact_d2(Xc, cap, g, (long long)C.off + j) < c_ff.rc2_pl[ti][tj];
-          });
-          if (plb != ((e & (int)kPL) != 0)) A.nl[row + k] = e ^ (int)kPL;
-        }
-      }
-    }
-  }
-  if (C.terms & SOP_TERM_FENE) {
-    // FENE (energy.cpp:402-447); d^2 - r0^2 in two-float arithmetic so the
-    // stretch dev = (d^2 - r0^2)/(d + r0) keeps FP32 relative accuracy.
-    for (int k = lane; k < bnd_cnt; k += G) {
-      const int4 b = bn;
-      if (k + G < bnd_cnt) bn = A.bnd[tp.y + k + G];
-      const int j = b.x;
-      const float r0 = __int_as_float(b.y), r0h = __int_as_float(b.z), r0l = __int_as_float(b.w);
-      const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
-      float dx, dy, dz, d2;
-      const float diff = d2_minus(hi, lo, hj, lj, r0h, r0l, dx, dy, dz, d2);  // d^2 - r0^2
-      const float d = sqrtf(d2);
-      const float dev = __fdividef(diff, d + r0);
-      const float den = 1.0f - dev * dev * C.inv_R0sq;
-      if (!(den > 0.f)) st |= SOP_ST_FENE;
-      const float temp = __fdividef(-C.kbnd * dev, d * den);
-      add(-temp * dx, -temp * dy, -temp * dz);
-    }
-  }
-  if (C.terms & SOP_TERM_ANGLE) {
-    // i,i+2 soft-sphere repulsion (energy.cpp:354-400)
-    for (int k = lane; k < ang_cnt; k += G) {
-      const int j = an;
-      if (k + G < ang_cnt) an = A.ang[tp.z + k + G];
-      const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
-      const float dx = (hj.x - hi.x) + (lj.x - lo.x);
-      const float dy = (hj.y - hi.y) + (lj.y - lo.y);
-      const float dz = (hj.z - hi.z) + (lj.z - lo.z);
-      const float d2 = dx * dx + dy * dy + dz * dz;
-      const float d4 = d2 * d2, d8 = d4 * d4;
-      const float co = __fdividef(C.fang, d8);
-      add(-co * dx, -co * dy, -co * dz);
-    }
-  }
+// The bead the contributions act on.
+struct BeadRef {
+  float4 hi, lo;  // staged position (hi, lo) with the type / chain codes
+  int i, ti;      // index in the replica, bead type
+  long long g;    // packed index
+};
 
-  // exact cross-lane sum of the fixed-point partials
-  if (!(mag <= kFixMax)) st |= SOP_ST_NONFINITE;  // NaN, inf or out of the fixed-point range
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) {
-    Fx += __shfl_xor_sync(gmask, Fx, o, G);
-    Fy += __shfl_xor_sync(gmask, Fy, o, G);
-    Fz += __shfl_xor_sync(gmask, Fz, o, G);
-  }
-  st |= __reduce_or_sync(gmask, st);
-  if (lane != 0) return;
+template <bool ST>
+__device__ __forceinline__ BeadRef bead_ref(const ItemCtx& C, const float4* S, int i) {
+  BeadRef b;
+  b.hi = ldp<ST>(S, 2 * i);
+  b.lo = ldp<ST>(S, 2 * i + 1);
+  b.i = i;
+  b.ti = (int)f2u(b.hi.w);
+  b.g = (long long)C.off + i;
+  return b;
+}
 
+// Native 12-6 attraction (energy.cpp:274-311) of native entry k (record e) of
+// bead b, and its pair-list bit for the next step.  The force vanishes at the
+// native distance, so (r0/d)^12 - (r0/d)^6 is formed from r0^2 - d^2 in
+// two-float arithmetic: with u = r0^2/d^2 - 1, s^3 - 1 = u (u^2 + 3u + 3).
+template <bool ST>
+__device__ __forceinline__ void native_entry(const DevArrays& A, const ItemCtx& C, const float4* S,
+                                             const BeadRef& b, int4 e, int k, bool upd,
+                                             FixAcc& acc) {
+  const int j = e.x & (int)kIdx;
+  const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
+  const float r0sq = __int_as_float(e.y);
+  float dx, dy, dz, d2;
+  const float diff = d2_minus(b.hi, b.lo, hj, lj, r0sq, __int_as_float(e.z), dx, dy, dz, d2);
+  if (e.x & (int)kPL) {
+    if (d2 >= (float)kTol * r0sq) {
+      const int tj = (int)f2u(hj.w);
+      const float inv = __fdividef(1.0f, d2);
+      const float u = -diff * inv;                     // s - 1, s = r0^2/d^2
+      const float s3m1 = u * fmaf(u, u + 3.0f, 3.0f);  // s^3 - 1
+      const float s3 = 1.0f + s3m1;
+      const float co = c_ff.fca[b.ti][tj] * inv * (s3 * s3m1);
+      acc.add(co * dx, co * dy, co * dz);
+    }
+  }
+  if (upd) {
+    bool plb = false;
+    if (e.x & (int)kNL) {
+      plb = within(d2, 6.25f * r0sq, kScreenMargin, [&] {
+        double rc = 2.5 * A.nat_r0[k], rc2 = rc * rc;
+        return exact_d2(A.X[C.cur], A.cap, b.g, (long long)C.off + j) < rc2;
+      });
+    }
+    if (plb != ((e.x & (int)kPL) != 0)) A.nat[k].x = e.x ^ (int)kPL;
+  }
+}
+
+// Non-native repulsion (energy.cpp:313-350) of list entry e at row slot idx,
+// and its pair-list bit for the next step.
+template <bool ST>
+__device__ __forceinline__ void nonnative_entry(const DevArrays& A, const ItemCtx& C, const float4* S,
+                                                const BeadRef& b, int e, long long idx, bool upd,
+                                                FixAcc& acc) {
+  const int j = e & (int)kIdx;
+  const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
+  const float dx = (hj.x - b.hi.x) + (lj.x - b.lo.x);
+  const float dy = (hj.y - b.hi.y) + (lj.y - b.lo.y);
+  const float dz = (hj.z - b.hi.z) + (lj.z - b.lo.z);
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  const int tj = (int)f2u(hj.w);
+  const float s2 = c_ff.s2[b.ti][tj];
+  if (e & (int)kPL) {
+    if (d2 >= s2 * (float)kTol) {
+      const float inv = __fdividef(1.0f, d2);
+      const float s = s2 * inv, s3 = s * s * s;
+      const float co = c_ff.fcr[b.ti][tj] * inv * (2.0f * s3 * s3 + s3);
+      acc.add(co * dx, co * dy, co * dz);
+    }
+  }
+  if (upd) {
+    const bool plb = within(d2, c_ff.rc2_pl_f[b.ti][tj], kScreenMargin, [&] {
+      return exact_d2(A.X[C.cur], A.cap, b.g, (long long)C.off + j) < c_ff.rc2_pl[b.ti][tj];
+    });
+    if (plb != ((e & (int)kPL) != 0)) A.nl[idx] = e ^ (int)kPL;
+  }
+}
+
+// FENE (energy.cpp:402-447) of bond record bd; d^2 - r0^2 in two-float
+// arithmetic so the stretch dev = (d^2 - r0^2)/(d + r0) keeps FP32 relative
+// accuracy.
+template <bool ST>
+__device__ __forceinline__ void bond_entry(const ItemCtx& C, const float4* S, const BeadRef& b, int4 bd,
+                                           FixAcc& acc) {
+  const int j = bd.x;
+  const float r0 = __int_as_float(bd.y), r0h = __int_as_float(bd.z), r0l = __int_as_float(bd.w);
+  const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
+  float dx, dy, dz, d2;
+  const float diff = d2_minus(b.hi, b.lo, hj, lj, r0h, r0l, dx, dy, dz, d2);  // d^2 - r0^2
+  const float d = sqrtf(d2);
+  const float dev = __fdividef(diff, d + r0);
+  const float den = 1.0f - dev * dev * C.inv_R0sq;
+  if (!(den > 0.f)) acc.st |= SOP_ST_FENE;
+  const float temp = __fdividef(-C.kbnd * dev, d * den);
+  acc.add(-temp * dx, -temp * dy, -temp * dz);
+}
+
+// i,i+2 soft-sphere repulsion (energy.cpp:354-400) with partner j.
+template <bool ST>
+__device__ __forceinline__ void angle_entry(const ItemCtx& C, const float4* S, const BeadRef& b, int j,
+                                            FixAcc& acc) {
+  const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
+  const float dx = (hj.x - b.hi.x) + (lj.x - b.lo.x);
+  const float dy = (hj.y - b.hi.y) + (lj.y - b.lo.y);
+  const float dz = (hj.z - b.hi.z) + (lj.z - b.lo.z);
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  const float d4 = d2 * d2, d8 = d4 * d4;
+  const float co = __fdividef(C.fang, d8);
+  acc.add(-co * dx, -co * dy, -co * dz);
+}
+
+// The bead's update from its exact force sum: noise, pulling force, the
+// underdamped / overdamped step (FP64 position accumulation), the next
+// staging, the skin trigger, status bits.
+template <bool ST>
+__device__ __forceinline__ void bead_tail(const DevArrays& A, const ItemCtx& C, const float4* S,
+                                          const BeadRef& b, long long Fx, long long Fy, long long Fz,
+                                          int st) {
+  const long long cap = A.cap, g = b.g;
+  const int i = b.i;
+  const double* Xc = A.X[C.cur];
   float F[3] = {float_from_fixed(Fx), float_from_fixed(Fy), float_from_fixed(Fz)};
   if ((C.terms & SOP_TERM_RANDOM) && C.amp > 0.f) {
     float nrm[3];
@@ -1072,8 +1062,8 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   if (C.pull_f != 0.f && (i == C.pull_i || i == C.pull_j)) {
     const int o = (i == C.pull_i) ? C.pull_j : C.pull_i;
     const float4 ho = ldp<ST>(S, 2 * o), lo2 = ldp<ST>(S, 2 * o + 1);
-    float ux = (ho.x - hi.x) + (lo2.x - lo.x), uy = (ho.y - hi.y) + (lo2.y - lo.y),
-          uz = (ho.z - hi.z) + (lo2.z - lo.z);
+    float ux = (ho.x - b.hi.x) + (lo2.x - b.lo.x), uy = (ho.y - b.hi.y) + (lo2.y - b.lo.y),
+          uz = (ho.z - b.hi.z) + (lo2.z - b.lo.z);
     float inv = rsqrtf(ux * ux + uy * uy + uz * uz);
     F[0] -= C.pull_f * ux * inv; F[1] -= C.pull_f * uy * inv; F[2] -= C.pull_f * uz * inv;
   }
@@ -1116,11 +1106,11 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
         A.incr[c * cap + g] = inc;
         split_double(xn[c], h[c], l[c]);
       }
-      A.stage[nb][2 * g] = make_float4(h[0], h[1], h[2], hi.w);
-      A.stage[nb][2 * g + 1] = make_float4(l[0], l[1], l[2], lo.w);
+      A.stage[nb][2 * g] = make_float4(h[0], h[1], h[2], b.hi.w);
+      A.stage[nb][2 * g + 1] = make_float4(l[0], l[1], l[2], b.lo.w);
       if (C.mode == SOP_LIST_SKIN) {
-        const float4 b = A.xb[g];
-        const float ex = h[0] - b.x, ey = h[1] - b.y, ez = h[2] - b.z;
+        const float4 xb = A.xb[g];
+        const float ex = h[0] - xb.x, ey = h[1] - xb.y, ez = h[2] - xb.z;
         const float d2 = ex * ex + ey * ey + ez * ez;
         if (d2 > C.half_skin2) {
           A.rep[C.r].rebuild = 1;
@@ -1134,6 +1124,77 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   }
   if (!finite3(F[0], F[1], F[2])) st |= SOP_ST_NONFINITE;
   if (st) atomicOr(&A.rep[C.r].status, st);
+}
+
+// One bead on a group of G lanes: each lane takes every G-th native entry,
+// list quad, bond and angle (loaded one iteration ahead), the lanes' exact
+// partial sums are reduced with shuffles and lane 0 updates the bead.
+template <int G, bool ST>
+__device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, const float4* S,
+                                          int i, int lane, unsigned gmask) {
+  const BeadRef b = bead_ref<ST>(C, S, i);
+  const int4 tp = A.topo[b.g];
+  // the non-native row: rows start 32-byte aligned and hold a multiple of 8
+  // entries, so a lane reads four entries with one 16-byte load (never past
+  // the row); the lane's first quad is in flight during the natives
+  const int cnt = A.nl_cnt[b.g];
+  const long long row = C.nl_base + (long long)i * C.L;
+  const int4* row4 = reinterpret_cast<const int4*>(A.nl + row);
+  int4 e4n = make_int4(0, 0, 0, 0);
+  if (4 * lane < C.L) e4n = row4[lane];
+  const int nat_cnt = tp.w & 0xFFFF, bnd_cnt = (tp.w >> 16) & 0xFF, ang_cnt = (tp.w >> 24) & 0xFF;
+  int4 bn = make_int4(0, 0, 0, 0);
+  int an = 0;
+  if (lane < bnd_cnt) bn = A.bnd[tp.y + lane];
+  if (lane < ang_cnt) an = A.ang[tp.z + lane];
+  const bool upd = (C.phase == PH_FIRST || C.phase == PH_NORMAL) && C.mode != SOP_LIST_NONE;
+  FixAcc acc;
+  if (C.terms & SOP_TERM_VDW) {
+    int4 en = make_int4(0, 0, 0, 0);  // the lane's next native record, loaded one entry ahead
+    if (lane < nat_cnt) en = A.nat[tp.x + lane];
+    for (int k = lane; k < nat_cnt; k += G) {
+      const int4 e = en;
+      if (k + G < nat_cnt) en = A.nat[tp.x + k + G];
+      native_entry<ST>(A, C, S, b, e, tp.x + k, upd, acc);
+    }
+    for (int q = lane; 4 * q < cnt; q += G) {
+      const int4 e4 = e4n;
+      if (4 * (q + G) < cnt) e4n = row4[q + G];
+      const int ev[4] = {e4.x, e4.y, e4.z, e4.w};
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int k = 4 * q + u;
+        if (k >= cnt) break;
+        nonnative_entry<ST>(A, C, S, b, ev[u], row + k, upd, acc);
+      }
+    }
+  }
+  if (C.terms & SOP_TERM_FENE) {
+    for (int k = lane; k < bnd_cnt; k += G) {
+      const int4 bd = bn;
+      if (k + G < bnd_cnt) bn = A.bnd[tp.y + k + G];
+      bond_entry<ST>(C, S, b, bd, acc);
+    }
+  }
+  if (C.terms & SOP_TERM_ANGLE) {
+    for (int k = lane; k < ang_cnt; k += G) {
+      const int j = an;
+      if (k + G < ang_cnt) an = A.ang[tp.z + k + G];
+      angle_entry<ST>(C, S, b, j, acc);
+    }
+  }
+  // exact cross-lane sum of the fixed-point partials
+  int st = acc.st | acc.range_status();
+  long long Fx = acc.x, Fy = acc.y, Fz = acc.z;
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    Fx += __shfl_xor_sync(gmask, Fx, o, G);
+    Fy += __shfl_xor_sync(gmask, Fy, o, G);
+    Fz += __shfl_xor_sync(gmask, Fz, o, G);
+  }
+  st |= __reduce_or_sync(gmask, st);
+  if (lane != 0) return;
+  bead_tail<ST>(A, C, S, b, Fx, Fy, Fz, st);
 }
 
 // MB: resident CTAs per SM the register allocation is sized for (2 or 3)
