@@ -7,7 +7,7 @@ single-kernel captures).  Run as
     PYTHONPATH=sop-cpu_gb300 python -m sop_gb300.cases globule --steps 3
 
 mix      512 replicas, N log-uniform 30-1500 (seed 2000), T 0.4-0.9, skin lists
-         (2.0 A): the batched step workload; one CUDA-graph-free batched step
+         (3.0 A): the batched step workload; one CUDA-graph-free batched step
          per --steps.
 build    one 1500-bead chain, neighbor list rebuilt before every step (nnlup 1):
          every prologue is a full list build.
@@ -33,7 +33,7 @@ WORKLOAD_SCRIPT = [("set", "zeta", "50"), ("set", "t_step", "0.05"), ("set", "te
                    ("set", "boxl", "2000"), ("set", "ncell", "250"), ("set", "run", "1")]
 
 
-def mix_engine(count=512, lo=30, hi=1500, skin=2.0, every_step=False, **cfg):
+def mix_engine(count=512, lo=30, hi=1500, skin=3.0, every_step=False, **cfg):
     systems, temps = S.mixed_batch(count, lo, hi, seed=2000)
     nb = sum(s.nbead for s in systems)
     eng = Engine(0, max_beads=max(1 << 16, int(nb * 1.3)), max_replicas=count + 16,

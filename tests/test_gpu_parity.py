@@ -247,6 +247,33 @@ def test_thermostat_matches_oracle(eng):
         eng.remove(r)
 
 
+def test_many_replicas_per_prep_cta():
+    """700 small replicas: every prep CTA owns two or three of them, hundreds
+    of producers publish build units while others consume, skin and cadence
+    rebuilds interleave.  A sample of the replicas equals the same replica run
+    alone, bit for bit (noise on)."""
+    from sop_gb300 import _lib as Lb
+    count = 700
+    sizes = [30 + (k * 37) % 90 for k in range(count)]
+    xyzs = Lb.synth_many([(52000 + k, n) for k, n in enumerate(sizes)])
+    systems = [S.system_from_xyz(x) for x in xyzs]
+    params = [make_params(script(temp=str(0.4 + 0.001 * (k % 400))), seed=5200 + k,
+                          list_mode="skin" if k % 2 else "neighborlist", skin=1.0)
+              for k in range(count)]
+    sample = [0, 1, 151, 302, 455, 699]
+    with Engine(0, max_beads=1 << 17, max_replicas=count + 8, max_list_entries=1 << 24) as e:
+        ids = [e.add(s, p) for s, p in zip(systems, params)]
+        e.run(200)
+        got = {k: e.state(ids[k])[1] for k in sample}
+        assert all(e.status(r)[0] == 0 for r in ids)
+    with Engine(0, max_beads=1 << 12, max_replicas=4, max_list_entries=1 << 20) as e:
+        for k in sample:
+            r = e.add(systems[k], params[k])
+            e.run(200)
+            np.testing.assert_array_equal(e.state(r)[1], got[k])
+            e.remove(r)
+
+
 def test_batch_invariance_with_noise(eng):
     """Each replica alone and inside a mix of uneven sizes: bit-identical,
     noise on (counter-based streams keyed by replica seed)."""
