@@ -821,9 +821,13 @@ __global__ void __launch_bounds__(kBuildThreads, 2) k_prep(DevArrays A, const in
     }
     __syncthreads();
   }
-  __threadfence();
+  // one fence after the barrier orders every unit this CTA queued (and the
+  // descriptor fields its threads wrote) before the producer-done signal
   __syncthreads();
-  if (threadIdx.x == 0) atomicAdd(A.pro_done, 1);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(A.pro_done, 1);
+  }
 
   // B. consumers
   for (;;) {
