@@ -242,8 +242,9 @@ int sop_last_run_timing(sop_engine* e, double* total_ms, double* step_kernel_ms,
  * prologue (bookkeeping + list builds + output-step energies). */
 int sop_profile_steps(sop_engine* e, int64_t nsteps, double* step_kernel_ms, double* prologue_ms);
 /* The same run split per kernel, mean ms per step: ms[0] launch gap before
- * the prologue (~0), ms[1] k_prologue (bookkeeping + cell binning), ms[2]
- * k_build (list slices, energies, observables), ms[3] k_step. */
+ * the preparation (~0), ms[1] k_prep (bookkeeping, cell binning, list slices,
+ * energies, observables: one kernel), ms[2] the gap after it (~0), ms[3]
+ * k_step. */
 int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms);
 
 /* The energies the last output step computed (step t with t % nup == 0 or the
@@ -292,7 +293,8 @@ typedef struct sop_server sop_server;
 typedef struct sop_server_config {
   sop_engine_config engine;
   int max_active;          /* replica slots in flight (0 = 1024)              */
-  int64_t memory_budget;   /* device bytes admissions may use (0 = 80% free)  */
+  int64_t memory_budget;   /* device bytes admissions may use (0 = no budget:
+                              the engine's arenas are the only limit)        */
   int chunk_steps;         /* steps between admission/retirement points (0=200) */
 } sop_server_config;
 typedef struct sop_request_result {
@@ -307,10 +309,12 @@ typedef struct sop_request_result {
 } sop_request_result;
 int sop_server_create(const sop_server_config* cfg, sop_server** out);
 int sop_server_destroy(sop_server* s);
-/* queue a request; the desc arrays are copied. */
+/* queue a request; the system is prepared on the host (topology, row sizing,
+ * device bytes) and the desc arrays need not outlive the call. */
 int sop_server_submit(sop_server* s, const sop_system_desc* d, int64_t nsteps, int64_t* request_id);
-/* admit, advance one chunk, retire; returns the number of requests still
- * queued or running in *pending. */
+/* end the chunk the previous pump launched, retire the requests it finished,
+ * admit queued requests, launch the next chunk and return while it runs;
+ * *pending = requests still queued or running. */
 int sop_server_pump(sop_server* s, int* pending);
 /* completed requests since the last call */
 int sop_server_poll(sop_server* s, sop_request_result* out, int cap, int* n);

@@ -238,8 +238,8 @@ class Engine:
         return s.value, p.value
 
     def profile_split(self, nsteps: int):
-        """Mean ms per step of k_prologue (bookkeeping + binning), k_build and
-        k_step (CUDA events)."""
+        """Mean ms per step of the preparation (k_prep: bookkeeping, binning,
+        list builds), the gap after it and k_step (CUDA events)."""
         out = (C.c_double * 4)()
         L.check(L.lib().sop_profile_steps_ex(self.h, int(nsteps), out), "sop_profile_steps_ex")
         return {"prologue": out[0] + out[1], "build": out[2], "step": out[3]}
