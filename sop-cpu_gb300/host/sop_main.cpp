@@ -13,8 +13,10 @@
 // and writes what the reference writes every nup steps: a row of ufname
 // (default update.out, appended: "istep T kinT e_bnd e_ang_ss e_vdw_rr
 // rna_etot Q contct_nat rgsq"), the coordinates (cfname, unccfname) and the
-// velocities (vfname).  The binary trajectory files and the reference's
-// sequential random stream are not reproduced: noise comes from the engine's
+// velocities (vfname), and a frame appended to each trajectory file (binfname,
+// uncbinfname; text frames, as record_traj writes them, starting with the
+// initial coordinates).  The reference's sequential random stream is not
+// reproduced: noise comes from the engine's
 // counter-based stream keyed by -100-run.  A vdw file listing fewer non-native
 // candidates than all pairs |i-j| > 2 is honoured through exclusions.
 #include <cmath>
@@ -77,7 +79,8 @@ struct Settings {
   int nup = 1000, nnlup = 50, run = 1, sim_type = 1;
   int neighborlist = 0, celllist = 0, restart = 0, rgen_restart = 0;
   std::string ufname = "update.out", cfname = "coord.out", unccfname = "unccoord.out",
-              vfname = "veloc.out", rcfname = "restart_c.dat";
+              vfname = "veloc.out", rcfname = "restart_c.dat", binfname = "traj.bin",
+              uncbinfname = "traj_uncorrected.bin";
 
   void integ() {  // params.cpp:22-27
     a1 = h * (1.0 - zeta * halfh);
@@ -122,6 +125,10 @@ struct Settings {
       unccfname = val;
     } else if (key == "vfname") {
       vfname = val;
+    } else if (key == "binfname") {
+      binfname = val;
+    } else if (key == "uncbinfname") {
+      uncbinfname = val;
     } else if (key == "cutofftype") {
       if (val == "neighborlist") neighborlist = 1;
       else if (val == "celllist") celllist = 1;
@@ -256,6 +263,15 @@ void write_coords(const std::string& fname, const std::vector<double>& x, int n)
   std::fclose(f);
 }
 
+// record_traj (io.cpp:280-303): one "%f %f %f" line per bead appended to the
+// file; despite the ".bin" default names the frames are text.
+void append_frame(const std::string& fname, const std::vector<double>& x, int n) {
+  FILE* f = std::fopen(fname.c_str(), "a");
+  if (!f) return;
+  for (int i = 0; i < n; i++) std::fprintf(f, "%f %f %f\n", x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+  std::fclose(f);
+}
+
 bool read_coords(const std::string& fname, std::vector<double>& x, int n) {
   std::ifstream in(fname);
   if (!in) return false;
@@ -289,6 +305,7 @@ int main(int argc, char** argv) {
   sop_engine* eng = nullptr;
   int rep = -1;
   std::vector<double> xyz, unc, vel;
+  bool first_run = true;  // the reference's static first_time (sop.cpp:102)
   for (const Command& c : cmds) {
     if (c.cmd == "load") {
       if (!load(c, top)) {
@@ -345,6 +362,12 @@ int main(int argc, char** argv) {
         istep = S.istep_restart + 1.0;
         if (S.rgen_restart) check(sop_replica_set_step(eng, rep, (int64_t)S.istep_restart), "set_step");
       }
+      if (first_run && !S.rgen_restart) {  // sop.cpp:149-152: the starting frame
+        check(sop_replica_get_state(eng, rep, xyz.data(), unc.data(), vel.data()), "get_state");
+        append_frame(S.binfname, xyz, n);
+        append_frame(S.uncbinfname, unc, n);
+      }
+      first_run = false;
       const long long nsteps = (long long)(S.nstep - istep + 1.0);
       if (nsteps <= 0) continue;
       FILE* uf = std::fopen(S.ufname.c_str(), "a");
@@ -384,6 +407,8 @@ int main(int argc, char** argv) {
           std::fprintf(uf, "%.0lf %f %f %f %f %f %f %f %d %f\n", istep - 1.0 + (double)L, S.T, o[3],
                        e[0], e[1], e[2], e[5], o[0], (int)o[1], o[2]);
           std::fflush(uf);
+          append_frame(S.binfname, xyz, n);
+          append_frame(S.uncbinfname, unc, n);
           write_coords(S.cfname, xyz, n);
           write_coords(S.unccfname, unc, n);
           write_coords(S.vfname, vel, n);

@@ -13,6 +13,8 @@ the reference's file formats, and stores inputs and outputs as .npz files:
   traj_*      state, energies, observables after 100 noise-free iterations
   cell_*      cell-list mode lists at set-up
   sd_update   sop.x update.out rows of a T=0 (steepest-descent) run
+  sd_unc      its final unccoord.out coordinates
+  sd_traj*    its traj.bin / traj_uncorrected.bin frames (initial + every nup)
 
     make -C oracle ref && python tests/golden/make_golden.py
 """
@@ -99,6 +101,9 @@ def one(seed, n):
         rows = [list(map(float, l.split())) for l in open(os.path.join(d, "update.out"))]
         rec["sd_update"] = np.array(rows)
         rec["sd_unc"] = np.loadtxt(os.path.join(d, "unccoord.out"))[:, 1:]
+        # record_traj's text frames (io.cpp:280-303): the start, then one per nup
+        rec["sd_traj"] = np.loadtxt(os.path.join(d, "traj.bin"))
+        rec["sd_traj_unc"] = np.loadtxt(os.path.join(d, "traj_uncorrected.bin"))
     np.savez_compressed(os.path.join(OUT, "sop_golden_N%d.npz" % n), **rec)
     print("wrote N=%d" % n)
 

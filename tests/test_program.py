@@ -2,7 +2,7 @@
 script and data files in, the same update.out rows and coordinate files out.
 Against sop.x's own output for a T = 0 (steepest-descent) run, carried by the
 golden fixtures: rows within 1e-5 relative (2e-6 absolute, the printed
-precision), final coordinates within 1e-5 A."""
+precision), final coordinates and every trajectory frame within 1e-5 A."""
 import glob
 import os
 import subprocess
@@ -49,8 +49,16 @@ def test_program_matches_reference_program(path):
         assert p.returncode == 0, p.stderr
         rows = np.array([list(map(float, l.split())) for l in open(os.path.join(d, "update.out"))])
         unc = np.loadtxt(os.path.join(d, "unccoord.out"))[:, 1:]
+        traj = np.loadtxt(os.path.join(d, "traj.bin"))
+        traj_unc = np.loadtxt(os.path.join(d, "traj_uncorrected.bin"))
     want = g["sd_update"]
     assert rows.shape == want.shape
     np.testing.assert_array_equal(rows[:, 0], want[:, 0])          # istep
     np.testing.assert_allclose(rows[:, 1:], want[:, 1:], rtol=1e-5, atol=2e-6)
     np.testing.assert_allclose(unc, g["sd_unc"], rtol=0, atol=1e-5)
+    # record_traj frames: the start (printed from the same input, so equal) and one per nup
+    n = len(g["xyz"])
+    assert traj.shape == g["sd_traj"].shape and traj_unc.shape == g["sd_traj_unc"].shape
+    np.testing.assert_array_equal(traj_unc[:n], g["sd_traj_unc"][:n])
+    np.testing.assert_allclose(traj_unc, g["sd_traj_unc"], rtol=0, atol=1e-5)
+    np.testing.assert_allclose(traj, g["sd_traj"], rtol=0, atol=1e-5)
