@@ -139,6 +139,10 @@ typedef struct sop_engine_config {
                             steps; forces and energies are exact integer sums,
                             so trajectories do not depend on it (0 = 50,
                             <0 = off)                                         */
+  int lean_prep;         /* a step's preparation kernel skips its work-queue
+                            phase when the previous step flagged no possible
+                            work (no skin trigger, output, observables or
+                            cadence build): 0 = on, <0 = off (same results)   */
 } sop_engine_config;
 
 /* ---- engine -------------------------------------------------------------- */
@@ -154,6 +158,9 @@ int sop_system_bytes(const sop_engine* e, const sop_system_desc* d, int64_t* byt
 int sop_engine_free_bytes(const sop_engine* e, int64_t* bytes);
 /* kernels launched by this engine since creation (all entry points) */
 int sop_engine_launches(const sop_engine* e, int64_t* launches);
+/* preparation launches that skipped the work-queue phase but found queued work
+ * all the same and ran it in one CTA (correct, slower; expected to stay 0) */
+int sop_engine_prep_fallbacks(sop_engine* e, int64_t* count);
 
 /* ---- replicas ------------------------------------------------------------- */
 /* Upload a system; builds its lists at the initial positions (the set-up of

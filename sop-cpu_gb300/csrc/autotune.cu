@@ -88,7 +88,7 @@ int set_lists(sop_engine* e, const std::vector<int>& ids, double skin, double ed
   }
   TK(cudaMemcpyAsync(e->d_pack_ids, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice,
                      e->stream));
-  TK(launch_prologue(e->A, e->d_pack_ids, (int)ids.size(), nullptr, 1, -1,
+  TK(launch_prologue(e->A, e->d_pack_ids, (int)ids.size(), nullptr, 1, -1, 1,
                      2 * e->prop.multiProcessorCount, e->stream));
   e->launches += kPrologueLaunches;
   rc = fetch_reps(e, reps);

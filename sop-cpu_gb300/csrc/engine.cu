@@ -223,6 +223,7 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
     if (cfg_in->step_min_blocks > 0) cfg.step_min_blocks = cfg_in->step_min_blocks;
     if (cfg_in->step_strategy > 0) cfg.step_strategy = cfg_in->step_strategy;
     if (cfg_in->group_rebuild_pct != 0) cfg.group_rebuild_pct = cfg_in->group_rebuild_pct;
+    cfg.lean_prep = cfg_in->lean_prep < 0 ? -1 : 0;
   }
   if (cfg.group_rebuild_pct < 0 || cfg.group_rebuild_pct >= 100) cfg.group_rebuild_pct = 0;
   if (cfg.step_strategy != 1) cfg.step_strategy = 0;
@@ -278,10 +279,11 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(dalloc(&A.pairs_out, e->pairs_cap));
   CK(dalloc(&A.pairs_cnt, 1));
   CK(dalloc(&A.err, 1));
-  // {next item, finished warps, any_rebuild}
-  CK(dalloc(&A.step_ctr, 3));
-  CK(cudaMemsetAsync(A.step_ctr, 0, 3 * sizeof(int), e->stream));
+  // {next item, finished warps, any_rebuild, prep flags (3)}
+  CK(dalloc(&A.step_ctr, 6));
+  CK(cudaMemsetAsync(A.step_ctr, 0, 6 * sizeof(int), e->stream));
   A.any_rebuild = A.step_ctr + 2;
+  A.prep_flag = A.step_ctr + 3;
   // grouped skin rebuilds: replicas past this fraction of their trigger
   // distance rebuild together with one that must (0 = off)
   A.group_frac2 = cfg.group_rebuild_pct > 0
@@ -385,6 +387,16 @@ extern "C" int sop_engine_sync(sop_engine* e) {
 extern "C" int sop_engine_launches(const sop_engine* e, int64_t* n) {
   if (!e || !n) return SOP_ERR_ARG;
   *n = e->launches;
+  return SOP_OK;
+}
+
+extern "C" int sop_engine_prep_fallbacks(sop_engine* e, int64_t* n) {
+  if (!e || !n) return SOP_ERR_ARG;
+  CK(cudaSetDevice(e->cfg.device));
+  int v = 0;
+  CK(cudaMemcpyAsync(&v, e->A.prep_flag + 2, sizeof v, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  *n = v;
   return SOP_OK;
 }
 
@@ -699,7 +711,7 @@ int sop::build_now(sop_engine* e, int r, int mode) {
   CK(cudaMemcpyAsync(e->d_ids + scratch_id(e, 0), &id, sizeof(int), cudaMemcpyHostToDevice,
                      e->stream));
   const int nsl = (R.n + e->A.slice_beads - 1) / e->A.slice_beads;
-  CK(launch_prologue(e->A, e->d_ids + scratch_id(e, 0), 1, nullptr, 1, mode,
+  CK(launch_prologue(e->A, e->d_ids + scratch_id(e, 0), 1, nullptr, 1, mode, 1,
                      std::min(nsl, 2 * e->prop.multiProcessorCount), e->stream));
   e->launches += kPrologueLaunches;
   CK(cudaStreamSynchronize(e->stream));
@@ -945,7 +957,7 @@ extern "C" int sop_replicas_admit(sop_engine* e, sop_prepared* const* p, const i
   if (m == 0) return SOP_ERR_FULL;
   // 2. one list build for all of them (sop.cpp:117-125: lists at the initial positions)
   CK(cudaMemcpyAsync(e->d_pack_ids, ids, m * sizeof(int), cudaMemcpyHostToDevice, e->stream));
-  CK(launch_prologue(e->A, e->d_pack_ids, m, nullptr, 1, -1, e->pro_grid, e->stream));
+  CK(launch_prologue(e->A, e->d_pack_ids, m, nullptr, 1, -1, 1, e->pro_grid, e->stream));
   e->launches += kPrologueLaunches;
   CK(cudaMemcpyAsync(e->h_reps, e->A.rep, sizeof(RepDev) * e->cfg.max_replicas,
                      cudaMemcpyDeviceToHost, e->stream));
@@ -1235,7 +1247,7 @@ int sop::refresh_layout(sop_engine* e) {
 // One step over given ids / items with host counts (single-replica paths).
 int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items,
                       int nitems, int max_staged, int step_grid, int pro_grid, bool fp64) {
-  CK(launch_prologue(e->A, d_ids, nrep, nullptr, 0, 0, pro_grid, e->stream));
+  CK(launch_prologue(e->A, d_ids, nrep, nullptr, 0, 0, 1, pro_grid, e->stream));
   if (fp64)
     CK(launch_step64(e->A, d_items, nitems, nullptr, step_grid, e->stream));
   else
@@ -1248,8 +1260,11 @@ int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem*
 
 // One batched step: k_prep (bookkeeping, binning, list slices, energies, observables),
 // k_step, sized by the engine's fixed grids and the device-resident counts.
-int sop::enqueue_batched_step(sop_engine* e) {
+// full: the first step after host-side work (every later k_prep reads the
+// device-side work flags the previous one left).
+int sop::enqueue_batched_step(sop_engine* e, bool full) {
   CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0,
+                     (full || e->cfg.lean_prep < 0) ? 1 : 0,
                      e->pro_grid, e->stream));
   CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, e->max_staged,
                  e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy,
@@ -1334,7 +1349,7 @@ static int capture_graph(sop_engine* e) {
   CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
   int64_t before = e->launches;
   for (int s = 0; s < e->cfg.graph_steps; s++) {
-    int rc = enqueue_batched_step(e);
+    int rc = enqueue_batched_step(e, s == 0);
     if (rc) { cudaStreamEndCapture(e->stream, &g); return rc; }
   }
   e->graph_launches = e->launches - before;
@@ -1365,7 +1380,7 @@ int sop::run_batched(sop_engine* e, int64_t nsteps, bool timed) {
     e->launches += e->graph_launches;
   }
   for (int64_t k = full * S; k < iters; k++) {
-    rc = enqueue_batched_step(e);
+    rc = enqueue_batched_step(e, k == full * S);
     if (rc) return rc;
   }
   // observables are computed on demand (sop_observables), not at run end
@@ -1450,7 +1465,7 @@ extern "C" int sop_run_chunk_begin(sop_engine* e, int64_t steps) {
     e->launches += e->graph_launches;
   }
   for (int64_t k = steps / S * S; k < steps; k++) {
-    rc = enqueue_batched_step(e);
+    rc = enqueue_batched_step(e, k == steps / S * S);
     if (rc) return rc;
   }
   CK(cudaEventRecord(e->ev[1], e->stream));
@@ -1505,7 +1520,7 @@ int sop::run_steps(sop_engine* e, int64_t steps, float* ms) {
     e->launches += e->graph_launches;
   }
   for (int64_t k = steps / S * S; k < steps; k++) {
-    rc = enqueue_batched_step(e);
+    rc = enqueue_batched_step(e, k == steps / S * S);
     if (rc) return rc;
   }
   CK(cudaEventRecord(e->ev[1], e->stream));
@@ -1582,7 +1597,7 @@ extern "C" int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms) {
   for (int64_t s = 0; s < iters; s++) {
     cudaEvent_t* E = &ev[kE * s];
     CK(cudaEventRecord(E[0], e->stream));
-    CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0, e->pro_grid,
+    CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0, s == 0, e->pro_grid,
                        e->stream, E[1], E[2]));
     CK(cudaEventRecord(E[3], e->stream));
     CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, e->max_staged,
@@ -1635,7 +1650,7 @@ extern "C" int sop_run_host(sop_engine* e, const double* xyz_in, const double* v
   if (vel_in) CK(h2d(e->d_pack_vel, vel_in, 3 * total, e->stream));
   CK(launch_scatter_state(e->A, e->d_pack_ids, nrep, e->d_pack_off, e->d_pack_xyz,
                           vel_in ? e->d_pack_vel : nullptr, e->stream));
-  CK(launch_prologue(e->A, e->d_pack_ids, nrep, nullptr, 1, -1, e->pro_grid, e->stream));
+  CK(launch_prologue(e->A, e->d_pack_ids, nrep, nullptr, 1, -1, 1, e->pro_grid, e->stream));
   e->launches += kPrologueLaunches;
   rc = run_batched(e, nsteps, false);
   if (rc) return rc;

@@ -122,7 +122,7 @@ void set_launch_shape(sop_engine* e, const LaunchShape& s);
 int enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items, int nitems,
                  int max_staged, int step_grid, int pro_grid, bool fp64);
 // one step of every active replica, sized only by device-resident counts
-int enqueue_batched_step(sop_engine* e);
+int enqueue_batched_step(sop_engine* e, bool full);
 int run_batched(sop_engine* e, int64_t nsteps, bool timed);
 inline int scratch_id(const sop_engine* e, int k) { return e->cfg.max_replicas + k; }
 }  // namespace sop

@@ -729,6 +729,15 @@ __device__ int decide_one(const DevArrays& A, int r, int force_build, int build_
     R->max_row = 0;
   }
   if (out && !need) push_units(A, r, U_ENERGY, 0, 1, Q.cur);
+  // work this replica may queue at the next step: the observables of this
+  // output step, the energies of an output step, a cadence build.  (A skin
+  // trigger raises any_rebuild in the step kernel; host-side changes make the
+  // next k_prep a full one.)
+  if (out || (ph != PH_FINAL &&
+              ((Q.nup > 0 && (Q.t + 1) % Q.nup == 0) ||
+               ((Q.mode == SOP_LIST_NEIGHBOR || Q.mode == SOP_LIST_CELL) &&
+                (Q.nnlup <= 1 || Q.inlup % Q.nnlup == 0)))))
+    A.prep_flag[1] = 1;
   return need ? (Q.mode | (prev << 8)) : -1;
 }
 
@@ -783,7 +792,7 @@ constexpr unsigned long long kQueueWaitNs = 2000000000ULL;  // 2 s: never expect
 __global__ void __launch_bounds__(kBuildThreads, 2) k_prep(DevArrays A, const int* rep_ids,
                                                           const int* nrep_dev, int nrep_host,
                                                           int force_build, int build_mode,
-                                                          int dyn_bytes) {
+                                                          int force_full, int dyn_bytes) {
   extern __shared__ __align__(16) unsigned char dyn[];
   __shared__ BuildSmem B;
   __shared__ int s_build[kBuildThreads];
@@ -793,6 +802,10 @@ __global__ void __launch_bounds__(kBuildThreads, 2) k_prep(DevArrays A, const in
   const int nrep = nrep_dev ? *nrep_dev : nrep_host;
   const int group = *A.any_rebuild;
   const int sb = A.slice_beads;
+  // lean launch: no replica can queue work this step (no skin trigger, no
+  // output, observables or cadence build flagged by the last k_prep), so the
+  // CTAs skip the consumer phase and its wait for every producer
+  const bool full = force_full || force_build || group || A.prep_flag[0];
 
   // A. producers
   const int mine = nrep > (int)blockIdx.x ? (nrep - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
@@ -824,54 +837,75 @@ __global__ void __launch_bounds__(kBuildThreads, 2) k_prep(DevArrays A, const in
   // one fence after the barrier orders every unit this CTA queued (and the
   // descriptor fields its threads wrote) before the producer-done signal
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (full && threadIdx.x == 0) {
     __threadfence();
     atomicAdd(A.pro_done, 1);
   }
 
-  // B. consumers
+  // B. consumers (a lean launch has none; see below)
+  bool consume = full;
   for (;;) {
-    if (threadIdx.x == 0) {
-      const int t = atomicAdd(A.unit_take, 1);
-      int4 w = make_int4(-1, 0, 0, 0);
-      const unsigned long long t0 = globaltimer_ns();
-      for (;;) {
-        if (t < min(ld_volatile(A.unit_cnt), A.unit_cap)) {
-          const int x = ld_volatile(&A.units[t].x);
-          if (x >= 0) {
+    for (; consume;) {
+      if (threadIdx.x == 0) {
+        const int t = atomicAdd(A.unit_take, 1);
+        int4 w = make_int4(-1, 0, 0, 0);
+        const unsigned long long t0 = globaltimer_ns();
+        for (;;) {
+          if (t < min(ld_volatile(A.unit_cnt), A.unit_cap)) {
+            const int x = ld_volatile(&A.units[t].x);
+            if (x >= 0) {
+              __threadfence();
+              w = make_int4(x, ld_volatile(&A.units[t].y), ld_volatile(&A.units[t].z),
+                            ld_volatile(&A.units[t].w));
+              A.units[t].x = -1;  // free for the next step
+              break;
+            }
+          } else if (ld_volatile(A.pro_done) == (int)gridDim.x) {
             __threadfence();
-            w = make_int4(x, ld_volatile(&A.units[t].y), ld_volatile(&A.units[t].z),
-                          ld_volatile(&A.units[t].w));
-            A.units[t].x = -1;  // free for the next step
+            if (t >= min(ld_volatile(A.unit_cnt), A.unit_cap)) break;  // drained
+            continue;
+          }
+          if (globaltimer_ns() - t0 > kQueueWaitNs) {  // never expected: record and stop
+            atomicOr(A.err, 2);
             break;
           }
-        } else if (ld_volatile(A.pro_done) == (int)gridDim.x) {
-          __threadfence();
-          if (t >= min(ld_volatile(A.unit_cnt), A.unit_cap)) break;  // drained
-          continue;
         }
-        if (globaltimer_ns() - t0 > kQueueWaitNs) {  // never expected: record and stop
-          atomicOr(A.err, 2);
-          break;
-        }
+        s_unit = w;
       }
-      s_unit = w;
+      __syncthreads();
+      const int4 w = s_unit;
+      if (w.x < 0) break;
+      run_unit(A, w, B, dyn, dyn_bytes, &s_last);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      __threadfence();
+      s_last = atomicAdd(A.unit_exit, 1) == (int)gridDim.x - 1;
     }
     __syncthreads();
-    const int4 w = s_unit;
-    if (w.x < 0) break;
-    run_unit(A, w, B, dyn, dyn_bytes, &s_last);
+    if (!s_last) return;
+    __threadfence();
+    if (consume || ld_volatile(A.unit_cnt) == 0) break;
+    // a lean launch that found work all the same (never expected): every
+    // producer is done, so the last CTA out becomes the queue's only consumer
+    // and results stay exact
+    if (threadIdx.x == 0) {
+      *A.pro_done = (int)gridDim.x;
+      *A.unit_exit = (int)gridDim.x - 1;
+      atomicAdd(A.prep_flag + 2, 1);
+    }
+    consume = true;
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(A.unit_exit, 1) == (int)gridDim.x - 1) {
-      __threadfence();
-      *A.unit_cnt = 0;
-      *A.unit_take = 0;
-      *A.pro_done = 0;
-      *A.unit_exit = 0;
-      if (!force_build) *A.any_rebuild = 0;
+    *A.unit_cnt = 0;
+    *A.unit_take = 0;
+    *A.pro_done = 0;
+    *A.unit_exit = 0;
+    if (!force_build) {
+      *A.any_rebuild = 0;
+      A.prep_flag[0] = ld_volatile(A.prep_flag + 1);
+      A.prep_flag[1] = 0;
     }
   }
 }
@@ -1800,7 +1834,7 @@ cudaError_t init_kernels(int optin_bytes, int sm_bytes) {
 }
 
 cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, const int* nrep_dev,
-                            int force_build, int build_mode, int grid, cudaStream_t s,
+                            int force_build, int build_mode, int full, int grid, cudaStream_t s,
                             cudaEvent_t after_decide, cudaEvent_t after_bin) {
   if (nrep <= 0) return cudaSuccess;
   cudaError_t e;
@@ -1818,7 +1852,7 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, co
   cfg.attrs = at;
   cfg.numAttrs = 1;
   if ((e = cudaLaunchKernelEx(&cfg, k_prep, A, rep_ids, nrep_dev, nrep, force_build, build_mode,
-                              g_prep_dyn)) != cudaSuccess)
+                              full, g_prep_dyn)) != cudaSuccess)
     return e;
   if (after_bin && (e = cudaEventRecord(after_bin, s)) != cudaSuccess) return e;
   return cudaSuccess;

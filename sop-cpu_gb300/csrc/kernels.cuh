@@ -51,6 +51,9 @@ struct DevArrays {
   int slice_beads;    // beads per list-build slice unit
   int* step_ctr;      // warp-task step kernel: {next item, finished warps}
   int* any_rebuild;   // a SKIN displacement trigger fired in the last step
+  // {[0] the next k_prep may have queued work, [1] the same, being decided by
+  //  this k_prep, [2] lean k_preps that found work all the same (diagnostic)}
+  int* prep_flag;
   float group_frac2;  // (grouping fraction of the trigger distance)^2; > 1 = no grouping
 };
 
@@ -96,8 +99,10 @@ cudaError_t init_kernels(int optin_bytes, int sm_bytes);
 // nrep / nitems: host counts (grid sizing); *_dev: the same counts in device
 // memory, read by the kernels when given (graphs survive layout changes).
 // after_decide / after_bin: events recorded before and after k_prep (profiling)
+// full: run the consumer phase whatever the device-side work flags say (the
+// first k_prep after any host-side change to replica state)
 cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, const int* nrep_dev,
-                            int force_build, int build_mode, int grid, cudaStream_t s,
+                            int force_build, int build_mode, int full, int grid, cudaStream_t s,
                             cudaEvent_t after_decide = nullptr, cudaEvent_t after_bin = nullptr);
 // min_blocks: the step-kernel variant whose registers are sized for 2 or 3
 // resident CTAs per SM

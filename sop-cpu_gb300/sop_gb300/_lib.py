@@ -77,6 +77,7 @@ class EngineConfig(C.Structure):
         ("lanes_per_bead", C.c_int), ("graph_steps", C.c_int),
         ("stage_limit", C.c_int), ("chunk_beads", C.c_int), ("build_slice_beads", C.c_int),
         ("step_min_blocks", C.c_int), ("step_strategy", C.c_int), ("group_rebuild_pct", C.c_int),
+        ("lean_prep", C.c_int),
     ]
 
 
@@ -108,6 +109,7 @@ _PROTOS = {
     "sop_system_bytes": (C.c_int, [VP, C.POINTER(SystemDesc), C.POINTER(C.c_int64)]),
     "sop_engine_free_bytes": (C.c_int, [VP, C.POINTER(C.c_int64)]),
     "sop_engine_launches": (C.c_int, [VP, C.POINTER(C.c_int64)]),
+    "sop_engine_prep_fallbacks": (C.c_int, [VP, C.POINTER(C.c_int64)]),
     "sop_replica_add": (C.c_int, [VP, C.POINTER(SystemDesc), IP]),
     "sop_replica_remove": (C.c_int, [VP, C.c_int]),
     "sop_replica_set_params": (C.c_int, [VP, C.c_int, C.POINTER(Params)]),

@@ -249,6 +249,12 @@ class Engine:
         L.check(L.lib().sop_engine_launches(self.h, C.byref(n)), "sop_engine_launches")
         return n.value
 
+    def prep_fallbacks(self) -> int:
+        """Lean preparation launches that found queued work (expected 0)."""
+        n = C.c_int64()
+        L.check(L.lib().sop_engine_prep_fallbacks(self.h, C.byref(n)), "sop_engine_prep_fallbacks")
+        return n.value
+
     def sync(self):
         L.check(L.lib().sop_engine_sync(self.h), "sop_engine_sync")
 
