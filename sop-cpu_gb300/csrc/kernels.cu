@@ -507,6 +507,10 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
     const int pre0 = incl - lsum;  // candidate index of this lane's first cell
     int carry = 0;  // sorted slot - candidate index of the cell running into the window
     int cnt = 0;    // warp-uniform
+    // pair-list entries fill the row from the front, the rest from the back, so
+    // the step kernel's warps pass the force code of a row's skin entries in
+    // step (the sums are exact, so entry order does not change any result)
+    int cntp = 0;   // warp-uniform: entries in the pair list
     for (int base = 0; base < total; base += 32) {
       // every non-empty cell that starts inside the window marks its first
       // position; a lane's cell is the last mark at or before it
@@ -571,9 +575,25 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
         }
       }
       const unsigned m = __ballot_sync(0xffffffffu, pass);
-      const int pos = cnt + __popc(m & lt_mask);
-      if (pass && pos < L) A.nl[row + pos] = j | (inp ? (int)kPL : 0);
+      const unsigned mp = __ballot_sync(0xffffffffu, pass && inp);
+      const int pos = inp ? cntp + __popc(mp & lt_mask)
+                          : L - 1 - ((cnt - cntp) + __popc(m & ~mp & lt_mask));
+      if (pass && pos >= 0 && pos < L) A.nl[row + pos] = j | (inp ? (int)kPL : 0);
       cnt += __popc(m);
+      cntp += __popc(mp);
+    }
+    if (cnt <= L && cnt > cntp) {
+      // move the back block [L - (cnt - cntp), L) down to cntp (dest <= src,
+      // 32 entries at a time, each chunk read before it is written)
+      __syncwarp();
+      const long long src = row + L - (cnt - cntp), dst = row + cntp;
+      for (int k0 = 0; k0 < cnt - cntp; k0 += 32) {
+        const int k = k0 + lane;
+        const int v = k < cnt - cntp ? A.nl[src + k] : 0;
+        __syncwarp();
+        if (k < cnt - cntp) A.nl[dst + k] = v;
+        __syncwarp();
+      }
     }
     if (lane == 0) {
       if (cnt > L) my_status |= SOP_ST_LIST_OVERFLOW;
