@@ -18,7 +18,8 @@ roofline   the fused step kernel: algorithmic bytes per launch over its
            CUDA-event duration against MEASURED_PEAKS.json hbm_gbs; traffic
            = DRAM bytes per launch of the same kernel on the same workload
            from the ncu capture summarized in profiles/k_step_mix512.md
-           (caches flushed before the captured pass).
+           (caches flushed before the captured pass); the same achieved GB/s
+           against the L2 bandwidth measured in the run.
 cpu_baseline  the CPU oracle (the reference algorithm restated in C) on a
            stratified sample of the replicas, all host threads.
 
@@ -380,6 +381,25 @@ def force_check(eng, ids, systems, count=4):
     return worst
 
 
+def measure_l2_gbs():
+    """L2 bandwidth of this GPU: a device copy of 24 MB (read + write, both
+    resident in the 129 MB L2), best of 30 after warm-up, CUDA events."""
+    import torch
+    a = torch.ones(6 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(5):
+        b.copy_(a)
+    best = float("inf")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(30):
+        e0.record()
+        b.copy_(a)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2 * a.numel() * 4 / (best / 1e3) / 1e9
+
+
 def flush_l2():
     import torch
     buf = getattr(flush_l2, "buf", None)
@@ -428,6 +448,7 @@ def run_gb300(args):
     algo = algorithmic_bytes(eng, ids, systems)
     peak, peak_kind = read_peaks()
     achieved = algo / (step_ms / 1e3) / 1e9
+    l2_gbs = measure_l2_gbs()
 
     # end to end through the host-buffer C call
     nb3 = 3 * beads
@@ -489,7 +510,9 @@ def run_gb300(args):
                      "traffic": read_traffic() if default_workload(args) else None,
                      "traffic_note": "ncu, caches flushed before the captured pass",
                      "kernel": "k_step (fused force + Langevin)", "kernel_ms": step_ms,
-                     "prologue_ms": pro_ms, "algorithmic_bytes_per_launch": algo},
+                     "prologue_ms": pro_ms, "algorithmic_bytes_per_launch": algo,
+                     "l2": {"peak": l2_gbs, "frac": achieved / l2_gbs,
+                            "peak_source": "measured here: 24 MB device copy, L2-resident"}},
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1:

@@ -339,8 +339,8 @@ int sop_synth_globule(uint64_t seed, int nchain, int chain_len, int compact_step
 
 /* ---- neighbor list without allocation ---------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
- * memory: code capturing a CUDA graph (cudaMalloc cannot be captured) and
- * hosts whose device memory belongs to their own pool.  Every input and
+ * memory: hosts whose device memory belongs to their own pool, and loops that
+ * cannot take the device-wide synchronization cudaMalloc / cudaFree may cause.  Every input and
  * output is a device pointer owned by the caller; the only other memory used
  * is a fixed static scratch array in the library (about 0.6 MB, held on each
  * GPU that loads the library until exit), sized for SOP_NOALLOC_MAX_BEADS.

@@ -1,9 +1,10 @@
 // Neighbor list of one system without any device allocation.
 //
-// For callers that cannot allocate device memory themselves: code that is
-// capturing a CUDA graph (cudaMalloc cannot be captured), and hosts whose
-// device memory is owned by their own pool or whose deployment forbids
-// allocation after start-up.  They pass device pointers for every input and
+// For callers that cannot allocate device memory themselves: hosts whose
+// device memory is owned by their own pool (a framework's caching allocator
+// that holds the GPU's memory), deployments that forbid allocation after
+// start-up, and latency-critical loops that cannot take the device-wide
+// synchronization a cudaMalloc or cudaFree may cause.  They pass device pointers for every input and
 // output; the binning scratch lives in one file-scope __device__ array of
 // fixed size (SOP_NOALLOC_MAX_BEADS beads), which every GPU that loads this
 // library holds until the process exits.

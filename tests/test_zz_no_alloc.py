@@ -1,6 +1,6 @@
 """sop_neighbor_list_noalloc: the neighbor list for callers that cannot
-allocate device memory (graph-capturing code, hosts that own all device
-memory through their own pool).  Every buffer here is allocated by the test
+allocate device memory (hosts that own all device memory through their own
+pool, loops that cannot take the synchronization an allocation may cause).  Every buffer here is allocated by the test
 (torch) and handed over as a device pointer; the library itself allocates
 nothing for this call.  Its pairs must equal, as integer sets, the list the
 engine's own entry points give (sop_update_neighbor_list +
