@@ -19,9 +19,15 @@ roofline   the fused step kernel: algorithmic bytes per launch over its
            = DRAM bytes per launch of the same kernel on the same workload
            from the ncu capture summarized in profiles/k_step_mix512.md
            (caches flushed before the captured pass); the same achieved GB/s
-           against the L2 bandwidth measured in the run.
+           against the L2 read bandwidth measured in the run.
 cpu_baseline  the CPU oracle (the reference algorithm restated in C) on a
            stratified sample of the replicas, all host threads.
+served     Poisson arrivals into the continuous-batching server: throughput,
+           p50 / p99 latency.
+large_system  a 50,000-bead globule: mixed and FP64 throughput, mixed-vs-FP64
+           force error and energy drift.
+single_system  one 3000-bead chain on its own (the plain single-system
+           path): throughput, force error against the oracle every 1000 steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -71,6 +77,10 @@ def parse():
     ap.add_argument("--large-chains", type=int, default=100,
                     help="single large system: chains x --large-len beads (0 = skip)")
     ap.add_argument("--large-len", type=int, default=500)
+    ap.add_argument("--single-len", type=int, default=3000,
+                    help="single-system leg: one chain of this many beads")
+    ap.add_argument("--single-steps", type=int, default=10000,
+                    help="single-system leg: steps, in windows of 1000 (0 = skip)")
     ap.add_argument("--large-steps", type=int, default=2000)
     return ap.parse_args()
 
@@ -349,55 +359,87 @@ def serve_stream(args, rank):
                       % (args.serve_rate, len(pool), lo, hi)}
 
 
+def force_err(eng, r, s):
+    """Normwise relative force error of replica r against the CPU oracle (the
+    reference's FP64 formulas) at its current state, lists rebuilt there on
+    both sides, random term off on both sides; r's parameters are restored."""
+    from oracle import oracle as O
+    from sop_gb300 import _lib as L
+    keep = eng.params(r)
+    p = eng.params(r)
+    p.force_terms = L.TERM_FENE | L.TERM_ANGLE | L.TERM_VDW
+    eng.set_params(r, p)
+    eng.neighbor_list(r)
+    eng.pair_list(r)
+    f = eng.force(r)
+    _, x, _ = eng.state(r)
+    eng.set_params(r, keep)
+    port = O.Port()
+    port.set_system(s)
+    for _, key, v in workload_script():
+        port.command(key, v)
+    port.set_coords(0, x)
+    port.set_coords(1, x)
+    port.set_force_terms(0, 1, 1, 1)
+    port.neighbor_list()
+    port.pair_list()
+    port.force_eval()
+    fr = port.coords(3)
+    return float(np.linalg.norm(f - fr) / np.linalg.norm(fr))
+
+
 def force_check(eng, ids, systems, count=4):
     """Force error of sampled replicas against the CPU oracle at their current
     state (random term off on both sides): max normwise relative error."""
-    from oracle import oracle as O
-    from sop_gb300 import _lib as L
     order = np.argsort([s.nbead for s in systems])
     pick = order[np.linspace(0, len(order) - 1, count).round().astype(int)]
-    worst = 0.0
-    for k in pick:
-        r, s = ids[k], systems[k]
-        p = eng.params(r)
-        p.force_terms = L.TERM_FENE | L.TERM_ANGLE | L.TERM_VDW
-        eng.set_params(r, p)
-        eng.neighbor_list(r)
-        eng.pair_list(r)
-        f = eng.force(r)
-        _, x, _ = eng.state(r)
-        port = O.Port()
-        port.set_system(s)
-        for _, key, v in workload_script():
-            port.command(key, v)
-        port.set_coords(0, x)
-        port.set_coords(1, x)
-        port.set_force_terms(0, 1, 1, 1)
-        port.neighbor_list()
-        port.pair_list()
-        port.force_eval()
-        fr = port.coords(3)
-        worst = max(worst, float(np.linalg.norm(f - fr) / np.linalg.norm(fr)))
-    return worst
+    return max(force_err(eng, ids[k], systems[k]) for k in pick)
+
+
+def single_system(args):
+    """One compact chain of --single-len beads (3000, seed 1000) on its own: the
+    plain single-system path (one replica, the reference's neighbor-list
+    cadence, nnlup 10, underdamped, T 0.6, noise on), --single-steps steps in
+    windows of 1000; after each window the force at the current state against
+    the CPU oracle (FP64 reference formulas), as the check every 1000 steps."""
+    from sop_gb300 import systems as S
+    from sop_gb300.engine import Engine, make_params
+    s = S.synth_chain(1000, args.single_len)
+    n = s.nbead
+    windows = max(1, args.single_steps // 1000)
+    with Engine(0, max_beads=max(1 << 14, 2 * n), max_replicas=4, max_list_entries=n * 400) as eng:
+        r = eng.add(s, make_params(workload_script(), seed=1000))
+        eng.run(50)  # warm
+        total, errs = 0.0, []
+        for _ in range(windows):
+            eng.run(1000)
+            total += eng.timing()[0]
+            errs.append(force_err(eng, r, s))
+        status = eng.status(r)[0]
+    return {"workload": "one compact chain of %d beads, neighbor-list cadence (nnlup 10), T 0.6" % n,
+            "steps": 1000 * windows, "bead_steps_per_s": n * 1000 * windows / (total / 1e3),
+            "force_rel_err_max": max(errs), "force_checks": len(errs), "status": status}
 
 
 def measure_l2_gbs():
-    """L2 bandwidth of this GPU: a device copy of 24 MB (read + write, both
-    resident in the 129 MB L2), best of 30 after warm-up, CUDA events."""
+    """L2 read bandwidth of this GPU: one reduction kernel that reads a 24 MB
+    buffer (L2-resident after a first pass) 40 times over -- rows of a
+    stride-0 view summed separately, so every row re-reads the whole buffer;
+    best of 10, CUDA events."""
     import torch
     a = torch.ones(6 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    b = torch.empty_like(a)
-    for _ in range(5):
-        b.copy_(a)
+    v = a.expand(40, a.numel())
+    for _ in range(3):
+        v.sum(dim=1)
     best = float("inf")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(30):
+    for _ in range(10):
         e0.record()
-        b.copy_(a)
+        v.sum(dim=1)
         e1.record()
         e1.synchronize()
         best = min(best, e0.elapsed_time(e1))
-    return 2 * a.numel() * 4 / (best / 1e3) / 1e9
+    return v.numel() * 4 / (best / 1e3) / 1e9
 
 
 def flush_l2():
@@ -485,6 +527,7 @@ def run_gb300(args):
     eng.close()
     served = serve_stream(args, rank) if args.serve_seconds > 0 else None
     large = large_system(args) if (args.large_chains > 0 and rank == 0) else None
+    single = single_system(args) if (args.single_steps > 0 and rank == 0) else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -504,6 +547,7 @@ def run_gb300(args):
                            "batched_over_plain": value / plain},
         "served": served,
         "large_system": large,
+        "single_system": single,
         "force_rel_err": ferr,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
@@ -512,7 +556,7 @@ def run_gb300(args):
                      "kernel": "k_step (fused force + Langevin)", "kernel_ms": step_ms,
                      "prologue_ms": pro_ms, "algorithmic_bytes_per_launch": algo,
                      "l2": {"peak": l2_gbs, "frac": achieved / l2_gbs,
-                            "peak_source": "measured here: 24 MB device copy, L2-resident"}},
+                            "peak_source": "measured here: a 24 MB L2-resident buffer read 40x in one reduction"}},
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1:
