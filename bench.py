@@ -421,25 +421,15 @@ def single_system(args):
             "force_rel_err_max": max(errs), "force_checks": len(errs), "status": status}
 
 
-def measure_l2_gbs():
-    """L2 read bandwidth of this GPU: one reduction kernel that reads a 24 MB
-    buffer (L2-resident after a first pass) 40 times over -- rows of a
-    stride-0 view summed separately, so every row re-reads the whole buffer;
-    best of 10, CUDA events."""
-    import torch
-    a = torch.ones(6 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    v = a.expand(40, a.numel())
-    for _ in range(3):
-        v.sum(dim=1)
-    best = float("inf")
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(10):
-        e0.record()
-        v.sum(dim=1)
-        e1.record()
-        e1.synchronize()
-        best = min(best, e0.elapsed_time(e1))
-    return v.numel() * 4 / (best / 1e3) / 1e9
+def measure_l2_gbs(device):
+    """L2 read bandwidth of this GPU from the library's probe: a 32 MB buffer
+    (L2-resident) read 40 times by one kernel with L1-bypassing 16-byte loads,
+    best of five launches."""
+    import ctypes as C
+    from sop_gb300 import _lib as L
+    g = C.c_double()
+    L.check(L.lib().sop_probe_l2_read(device, 32 << 20, 40, C.byref(g)), "sop_probe_l2_read")
+    return g.value
 
 
 def flush_l2():
@@ -490,7 +480,7 @@ def run_gb300(args):
     algo = algorithmic_bytes(eng, ids, systems)
     peak, peak_kind = read_peaks()
     achieved = algo / (step_ms / 1e3) / 1e9
-    l2_gbs = measure_l2_gbs()
+    l2_gbs = measure_l2_gbs(local)
 
     # end to end through the host-buffer C call
     nb3 = 3 * beads
@@ -556,7 +546,7 @@ def run_gb300(args):
                      "kernel": "k_step (fused force + Langevin)", "kernel_ms": step_ms,
                      "prologue_ms": pro_ms, "algorithmic_bytes_per_launch": algo,
                      "l2": {"peak": l2_gbs, "frac": achieved / l2_gbs,
-                            "peak_source": "measured here: a 24 MB L2-resident buffer read 40x in one reduction"}},
+                            "peak_source": "measured here: sop_probe_l2_read, 32 MB read 40x"}},
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1:

@@ -364,6 +364,13 @@ int sop_neighbor_list_noalloc(const double* xyz, int nbead, const int* bead_type
                               const int* nat_ptr, const int* nat_idx, int* pairs, int cap,
                               int* count, void* stream);
 
+/* ---- measurement probe -------------------------------------------------------------- */
+/* No counterpart in the reference.  L2 read bandwidth of `device` in GB/s: a
+ * buffer of `bytes` (1-96 MB, so it stays in L2) read `reps` times by one
+ * kernel with L1-bypassing 16-byte loads, best of five launches, CUDA events.
+ * The benchmark's denominator for kernels whose working set lives in L2. */
+int sop_probe_l2_read(int device, int64_t bytes, int reps, double* gbs);
+
 /* ---- host-side numerics self-checks (no GPU needed) ------------------------------- */
 /* split a double into the (hi, lo) float pair the engine stages */
 void sop_selftest_split(double x, float* hi, float* lo);

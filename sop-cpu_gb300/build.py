@@ -22,7 +22,7 @@ LIBDIR = os.path.join(HERE, "lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["csrc/kernels.cu", "csrc/engine.cu", "csrc/noalloc.cu", "csrc/autotune.cu",
-              "csrc/checkpoint.cu"]
+              "csrc/checkpoint.cu", "csrc/probe.cu"]
 CXX_SOURCES = ["csrc/server.cpp", "host/synth.cpp"]
 PROGRAM = "host/sop_main.cpp"
 

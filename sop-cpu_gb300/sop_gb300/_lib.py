@@ -110,6 +110,7 @@ _PROTOS = {
     "sop_engine_free_bytes": (C.c_int, [VP, C.POINTER(C.c_int64)]),
     "sop_engine_launches": (C.c_int, [VP, C.POINTER(C.c_int64)]),
     "sop_engine_prep_fallbacks": (C.c_int, [VP, C.POINTER(C.c_int64)]),
+    "sop_probe_l2_read": (C.c_int, [C.c_int, C.c_int64, C.c_int, C.POINTER(C.c_double)]),
     "sop_replica_add": (C.c_int, [VP, C.POINTER(SystemDesc), IP]),
     "sop_replica_remove": (C.c_int, [VP, C.c_int]),
     "sop_replica_set_params": (C.c_int, [VP, C.c_int, C.POINTER(Params)]),

@@ -110,3 +110,12 @@ def test_synth_is_seeded_and_chain_like():
     d = np.linalg.norm(a[:, None] - a[None], axis=-1)
     iu = np.triu_indices(200, 2)
     assert d[iu].min() > 4.0  # excluded-volume floor
+
+
+def test_l2_probe_rejects_bad_sizes_before_touching_a_device():
+    g = C.c_double(-1.0)
+    lib = L.lib()
+    assert lib.sop_probe_l2_read(0, 1000, 10, C.byref(g)) == -1        # under 1 MB
+    assert lib.sop_probe_l2_read(0, 200 << 20, 10, C.byref(g)) == -1   # over 96 MB
+    assert lib.sop_probe_l2_read(0, 32 << 20, 0, C.byref(g)) == -1     # no repetitions
+    assert lib.sop_probe_l2_read(0, 32 << 20, 10, None) == -1
