@@ -342,6 +342,14 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   CK(dalloc(&e->d_pack_xyz, 3 * cap));
   CK(dalloc(&e->d_pack_vel, 3 * cap));
   CK(dalloc(&e->d_pack_ids, cfg.max_replicas));
+  CK(dalloc(&e->d_reps_pack, cfg.max_replicas));
+  // energy slices: every replica's beads in kEnergySlice slices, plus one
+  // partial slice each
+  e->en_part_cap = cap / kEnergySlice + cfg.max_replicas + 16;
+  CK(dalloc(&A.en_part, 4 * e->en_part_cap));
+  CK(dalloc(&A.en_done, cfg.max_replicas + 4));
+  CK(cudaMemsetAsync(A.en_done, 0, sizeof(int) * (cfg.max_replicas + 4), e->stream));
+  CK(dalloc(&e->d_en_base, cfg.max_replicas + 4));
   CK(dalloc(&e->d_pack_off, cfg.max_replicas));
   // fixed launch shapes of the batched step (so captured graphs stay valid):
   // persistent step CTAs as many as fit, staging sized by the stage limit
@@ -366,7 +374,8 @@ extern "C" int sop_engine_destroy(sop_engine* e) {
                   A.exc_rng, A.nl_cnt, A.nl, A.nat, A.nat_r0, A.bnd, A.bnd_r0, A.ang, A.exc,
                   A.rep, A.pairs_out, A.pairs_cnt, A.err, A.units, A.unit_cnt, A.slice_done,
                   A.done_list, A.done_cnt, e->d_ids, e->d_items, e->d_items64, e->d_counts, e->d_pack_xyz,
-                  e->d_pack_vel, e->d_pack_ids, e->d_pack_off, A.bin_p, A.bin_sorted,
+                  e->d_pack_vel, e->d_pack_ids, e->d_pack_off, e->d_reps_pack, e->d_en_base,
+                  A.en_part, A.en_done, A.bin_p, A.bin_sorted,
                   A.bin_cell, A.cstart, A.ccur, A.bin_hdr, A.step_ctr};
   for (void* p : ptrs) cudaFree(p);
   if (e->h_rep) cudaFreeHost(e->h_rep);
@@ -896,6 +905,57 @@ static int place(sop_engine* e, const sop_prepared& P, int* replica) {
   return SOP_OK;
 }
 
+// Energy terms of replicas ids[0..n) (ids also on the device at d_ids): their
+// slice bases, then one launch of the sliced energy kernel.
+static int enqueue_energy(sop_engine* e, const int* ids, const int* d_ids, int n) {
+  std::vector<int> base(n);
+  long long tot = 0;
+  int mx = 0;
+  for (int k = 0; k < n; k++) {
+    const int ns = (e->reps[ids[k]].n + kEnergySlice - 1) / kEnergySlice;
+    base[k] = (int)tot;
+    tot += ns;
+    mx = std::max(mx, ns);
+  }
+  if (tot > e->en_part_cap) return SOP_ERR_STATE;  // sized for the bead capacity: never
+  CK(cudaMemcpyAsync(e->d_en_base, base.data(), n * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  CK(launch_energy(e->A, d_ids, e->d_en_base, n, mx, e->stream));
+  e->launches++;
+  return SOP_OK;
+}
+
+// Descriptors of replicas ids[0..n) packed into out[0..n) (one CTA each), so a
+// batch reads back n descriptors instead of the whole table; with `clear`, each
+// descriptor is zeroed after it is copied (removal).
+__global__ void k_pack_reps(RepDev* rep, const int* ids, int n, RepDev* out, int clear) {
+  static_assert(sizeof(RepDev) % sizeof(int) == 0, "descriptor copied as ints");
+  constexpr int kWords = (int)(sizeof(RepDev) / sizeof(int));
+  for (int k = blockIdx.x; k < n; k += gridDim.x) {
+    int* src = reinterpret_cast<int*>(rep + ids[k]);
+    int* dst = reinterpret_cast<int*>(out + k);
+    for (int w = threadIdx.x; w < kWords; w += blockDim.x) dst[w] = src[w];
+    if (clear) {
+      __syncthreads();
+      for (int w = threadIdx.x; w < kWords; w += blockDim.x) src[w] = 0;
+    }
+    __syncthreads();
+  }
+}
+
+// Read back the descriptors of ids[0..n) (ids already in d_pack_ids) into
+// h_reps[0..n); `clear` also zeroes them on the device.  Synchronizes.
+static int read_packed_reps(sop_engine* e, int n, int clear, int* err) {
+  k_pack_reps<<<std::min(n, 1024), 128, 0, e->stream>>>(e->A.rep, e->d_pack_ids, n, e->d_reps_pack,
+                                                        clear);
+  e->launches++;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(e->h_reps, e->d_reps_pack, sizeof(RepDev) * n, cudaMemcpyDeviceToHost,
+                     e->stream));
+  if (err) CK(cudaMemcpyAsync(err, e->A.err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return SOP_OK;
+}
+
 __global__ void k_begin_many(RepDev* rep, const int* ids, const long long* nsteps, int n) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n || nsteps[k] <= 0) return;
@@ -959,13 +1019,15 @@ extern "C" int sop_replicas_admit(sop_engine* e, sop_prepared* const* p, const i
   CK(cudaMemcpyAsync(e->d_pack_ids, ids, m * sizeof(int), cudaMemcpyHostToDevice, e->stream));
   CK(launch_prologue(e->A, e->d_pack_ids, m, nullptr, 1, -1, 1, e->pro_grid, e->stream));
   e->launches += kPrologueLaunches;
-  CK(cudaMemcpyAsync(e->h_reps, e->A.rep, sizeof(RepDev) * e->cfg.max_replicas,
-                     cudaMemcpyDeviceToHost, e->stream));
-  CK(cudaStreamSynchronize(e->stream));
+  int rc0 = read_packed_reps(e, m, 0, nullptr);
+  if (rc0) return rc0;
   // 3. rows longer than estimated grow (rare), then the run windows open
+  std::vector<int> grow_row(m, -1);  // h_reps is reused by the calls below
+  for (int q = 0; q < m; q++)
+    if (e->h_reps[q].status & SOP_ST_LIST_OVERFLOW) grow_row[q] = e->h_reps[q].max_row;
   for (int q = 0; q < m; q++) {
-    if (!(e->h_reps[ids[q]].status & SOP_ST_LIST_OVERFLOW)) continue;
-    int rc = grow_rows(e, ids[q], e->h_reps[ids[q]].max_row);
+    if (grow_row[q] < 0) continue;
+    int rc = grow_rows(e, ids[q], grow_row[q]);
     if (rc == SOP_OK) rc = rebuild_fit(e, ids[q], e->reps[ids[q]].params.list_mode);
     if (rc) {  // no room for its rows: nothing of this batch is admitted
       for (int w = 0; w < m; w++) sop_replica_remove(e, ids[w]);
@@ -1409,31 +1471,32 @@ extern "C" int sop_replica_start(sop_engine* e, int r, int64_t nsteps) {
 
 extern "C" int sop_replicas_retire(sop_engine* e, const int* ids, int n, double* energy6, double* obs5,
                                    int* status) {
-  if (!e || n < 0 || (n > 0 && !ids)) return SOP_ERR_ARG;
+  if (!e || n < 0 || (n > 0 && !ids) || n > e->cfg.max_replicas) return SOP_ERR_ARG;
   if (n == 0) return SOP_OK;
-  for (int k = 0; k < n; k++)
-    if (!live(e, ids[k])) return SOP_ERR_ARG;
+  std::vector<char> seen(e->cfg.max_replicas, 0);
+  for (int k = 0; k < n; k++) {
+    if (!live(e, ids[k]) || seen[ids[k]]) return SOP_ERR_ARG;  // each replica once
+    seen[ids[k]] = 1;
+  }
   if (e->chunk_open) return SOP_ERR_STATE;
   CK(cudaSetDevice(e->cfg.device));
   CK(cudaStreamSynchronize(e->stream));
-  // final energies and observables of all of them, then one read-back
+  // final energies and observables of all of them, then one packed read-back
+  // that also clears their descriptors (removal)
   CK(cudaMemcpyAsync(e->d_pack_ids, ids, n * sizeof(int), cudaMemcpyHostToDevice, e->stream));
-  CK(launch_energy(e->A, e->d_pack_ids, n, e->stream));
+  int rc_e = enqueue_energy(e, ids, e->d_pack_ids, n);
+  if (rc_e) return rc_e;
   CK(launch_observables(e->A, e->d_pack_ids, n, e->stream));
-  e->launches += 2;
-  CK(cudaMemcpyAsync(e->h_reps, e->A.rep, sizeof(RepDev) * e->cfg.max_replicas,
-                     cudaMemcpyDeviceToHost, e->stream));
+  e->launches++;
   int err = 0;
-  CK(cudaMemcpyAsync(&err, e->A.err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
-  CK(cudaStreamSynchronize(e->stream));
-  static const RepDev zero{};
+  const int rc = read_packed_reps(e, n, 1, &err);
+  if (rc) return rc;
   for (int k = 0; k < n; k++) {
-    const RepDev& d = e->h_reps[ids[k]];
+    const RepDev& d = e->h_reps[k];
     if (energy6) std::memcpy(energy6 + 6 * k, d.energy, sizeof d.energy);
     if (obs5) std::memcpy(obs5 + 5 * k, d.obs, sizeof d.obs);
     if (status) status[k] = d.status | (err ? 0x100 : 0);
-    // removal: descriptor cleared (queued), arenas returned
-    CK(cudaMemcpyAsync(e->A.rep + ids[k], &zero, sizeof zero, cudaMemcpyHostToDevice, e->stream));
+    // removal: the descriptor was cleared by the read-back, arenas returned
     sop::Replica& R = e->reps[ids[k]];
     e->beads.release(R.off, R.n);
     e->lists.release(R.nl_base, (long long)R.n * R.L);
@@ -1754,8 +1817,8 @@ extern "C" int sop_force_eval(sop_engine* e, int r, double* force_xyz) {
 extern "C" int sop_energy_eval(sop_engine* e, int r, double* out) {
   if (!e || !live(e, r)) return SOP_ERR_ARG;
   CK(cudaMemcpyAsync(e->d_ids + scratch_id(e, 0), &r, sizeof(int), cudaMemcpyHostToDevice, e->stream));
-  CK(launch_energy(e->A, e->d_ids + scratch_id(e, 0), 1, e->stream));
-  e->launches++;
+  int rc_e = enqueue_energy(e, &r, e->d_ids + scratch_id(e, 0), 1);
+  if (rc_e) return rc_e;
   RepDev d;
   int rc = get_rep(e, r, &d);
   if (rc) return rc;

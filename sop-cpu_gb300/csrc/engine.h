@@ -59,7 +59,10 @@ struct sop_engine {
   sop::RangeAlloc beads, lists, nats, bnds, angs, excs, cells;
   std::vector<sop::Replica> reps;
   sop::RepDev* h_rep = nullptr;  // pinned staging for descriptor copies
-  sop::RepDev* h_reps = nullptr; // pinned copy of every descriptor (batched admission / retirement)
+  sop::RepDev* h_reps = nullptr; // pinned descriptors read back (all of them, or a packed batch)
+  sop::RepDev* d_reps_pack = nullptr;  // descriptors of one admission / retirement batch, packed
+  int* d_en_base = nullptr;       // energy kernel: first partial-sum slot of each replica of a batch
+  long long en_part_cap = 0;      // energy kernel: partial-sum slots (4 doubles each)
   int* h_done = nullptr;         // pinned: replicas whose window closed in the open chunk
   bool chunk_open = false;       // a chunk was launched and not yet waited for
   // batched layout

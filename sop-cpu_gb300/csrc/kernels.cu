@@ -1551,15 +1551,19 @@ __device__ void block_sum(double* v, int nv, double* red) {
   __syncthreads();
 }
 
-// Energy terms of one replica at positions X[buf] with the current pair list.
-__device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* red) {
-  const int n = R->n, off = R->off;
+// Energy sums of beads [b0, b1) of one replica at positions X[buf] with the
+// current pair list, this thread's share (beads b0 + tid, b0 + tid + blockDim,
+// ...; each pair counted once, from its lower-index bead): v = {FENE log sum,
+// angle sum, native sum, repulsion}.
+__device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b0, int b1,
+                             double v[4]) {
+  const int off = R->off;
   const long long cap = A.cap;
   const double* X = A.X[buf];
   const float4* S = A.stage[buf];
   double eb = 0, ea = 0, eatt = 0;
   long long erep_fx = 0;  // list-ordered sum: exact in fixed point (2^-40 kcal/mol)
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
     const long long gi = off + i;
     const int4 tp = A.topo[gi];
     const int nat_cnt = tp.w & 0xFFFF, bnd_cnt = (tp.w >> 16) & 0xFF, ang_cnt = (tp.w >> 24) & 0xFF;
@@ -1605,16 +1609,28 @@ __device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* r
       }
     }
   }
-  double v[4] = {eb, ea, eatt, (double)erep_fx * 9.094947017729282e-13};  // 2^-40
+  v[0] = eb;
+  v[1] = ea;
+  v[2] = eatt;
+  v[3] = (double)erep_fx * 9.094947017729282e-13;  // 2^-40
+}
+
+// The replica's energy terms from the summed v of energy_terms.
+__device__ void energy_finish(RepDev* R, const double v[4]) {
+  R->energy[0] = -R->e_bnd_coeff * v[0];
+  R->energy[1] = v[1];
+  R->energy[3] = v[2];
+  R->energy[4] = v[3];
+  R->energy[2] = v[2] + v[3];
+  R->energy[5] = R->energy[0] + R->energy[1] + R->energy[2];
+}
+
+// Energy terms of one replica on one CTA (output steps, list-build closes).
+__device__ void replica_energy(const DevArrays& A, RepDev* R, int buf, double* red) {
+  double v[4];
+  energy_terms(A, R, buf, 0, R->n, v);
   block_sum(v, 4, red);
-  if (threadIdx.x == 0) {
-    R->energy[0] = -R->e_bnd_coeff * v[0];
-    R->energy[1] = v[1];
-    R->energy[3] = v[2];
-    R->energy[4] = v[3];
-    R->energy[2] = v[2] + v[3];
-    R->energy[5] = R->energy[0] + R->energy[1] + R->energy[2];
-  }
+  if (threadIdx.x == 0) energy_finish(R, v);
 }
 
 // K6: observables (sop.cpp:200-279) at positions X[buf] and the stored velocities.
@@ -1658,10 +1674,38 @@ __device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red)
   }
 }
 
-__global__ void __launch_bounds__(256) k_energy(DevArrays A, const int* rep_ids, int nrep) {
+// Energy terms of replicas rep_ids[0..nrep) on many CTAs: CTA (x, y) sums
+// slice x (kEnergySlice beads) of replica rep_ids[y] into en_part[slice_base[y]
+// + x]; the CTA that finishes the replica's last slice adds the slices' sums
+// in slice order (deterministic) and stores the terms.
+__global__ void __launch_bounds__(256) k_energy(DevArrays A, const int* rep_ids,
+                                                const int* slice_base, int nrep) {
   __shared__ double red[4 * 256];
-  RepDev* R = &A.rep[rep_ids[blockIdx.x]];
-  replica_energy(A, R, R->cur, red);
+  __shared__ int s_last;
+  const int y = blockIdx.y;
+  RepDev* R = &A.rep[rep_ids[y]];
+  const int n = R->n;
+  const int nsl = (n + kEnergySlice - 1) / kEnergySlice;
+  const int x = blockIdx.x;
+  if (x >= nsl) return;  // the whole CTA: before any barrier
+  double v[4];
+  energy_terms(A, R, R->cur, x * kEnergySlice, min(n, (x + 1) * kEnergySlice), v);
+  block_sum(v, 4, red);
+  if (threadIdx.x == 0) {
+    double* p = A.en_part + 4LL * (slice_base[y] + x);
+    for (int q = 0; q < 4; q++) p[q] = v[q];
+    __threadfence();
+    s_last = atomicAdd(A.en_done + y, 1) == nsl - 1;
+    if (s_last) {
+      __threadfence();
+      double t[4] = {0, 0, 0, 0};
+      const volatile double* b = A.en_part + 4LL * slice_base[y];
+      for (int k = 0; k < nsl; k++)
+        for (int q = 0; q < 4; q++) t[q] += b[4 * k + q];
+      energy_finish(R, t);
+      A.en_done[y] = 0;
+    }
+  }
 }
 
 __global__ void __launch_bounds__(256) k_obs(DevArrays A, const int* rep_ids, int nrep) {
@@ -1909,9 +1953,10 @@ cudaError_t launch_step64(const DevArrays& A, const StepItem* items, int nitems,
   return cudaGetLastError();
 }
 
-cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s) {
-  if (nrep <= 0) return cudaSuccess;
-  k_energy<<<nrep, 256, 0, s>>>(A, rep_ids, nrep);
+cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, const int* slice_base, int nrep,
+                          int max_slices, cudaStream_t s) {
+  if (nrep <= 0 || max_slices <= 0) return cudaSuccess;
+  k_energy<<<dim3(max_slices, nrep), 256, 0, s>>>(A, rep_ids, slice_base, nrep);
   return cudaGetLastError();
 }
 

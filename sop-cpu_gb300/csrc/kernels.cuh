@@ -54,6 +54,10 @@ struct DevArrays {
   // {[0] the next k_prep may have queued work, [1] the same, being decided by
   //  this k_prep, [2] lean k_preps that found work all the same (diagnostic)}
   int* prep_flag;
+  // energy slices of sop_energy_eval / retirement: 4 partial sums per slice,
+  // and per replica of the batch the count of finished slices (reset to 0)
+  double* en_part;
+  int* en_done;
   float group_frac2;  // (grouping fraction of the trigger distance)^2; > 1 = no grouping
 };
 
@@ -80,6 +84,7 @@ struct StepItem {
 
 constexpr int kStageMax = 6144;       // beads staged in shared memory (192 KB)
 constexpr int kBuildThreads = 512;
+constexpr int kEnergySlice = 256;     // beads per CTA of the energy kernel
 // kernel launches of one step: k_prep (bookkeeping, binning, list builds), k_step
 constexpr int kPrologueLaunches = 1;
 constexpr int kStepLaunches = 2;
@@ -114,7 +119,10 @@ cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, c
 // the FP64-precision step over its own items (one thread per bead)
 cudaError_t launch_step64(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
                           int grid, cudaStream_t s);
-cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s);
+// energies of rep_ids[0..nrep) in slices of kEnergySlice beads; slice_base[k]:
+// replica k's first slot in en_part; max_slices: the most slices of any of them
+cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, const int* slice_base, int nrep,
+                          int max_slices, cudaStream_t s);
 cudaError_t launch_observables(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s);
 cudaError_t launch_pairlist(const DevArrays& A, int r, int off, int n, cudaStream_t s);
 // packed (x y z per bead, replicas back to back at 3*poff[k]) <-> device state
