@@ -1956,8 +1956,15 @@ cudaError_t launch_step64(const DevArrays& A, const StepItem* items, int nitems,
 cudaError_t launch_energy(const DevArrays& A, const int* rep_ids, const int* slice_base, int nrep,
                           int max_slices, cudaStream_t s) {
   if (nrep <= 0 || max_slices <= 0) return cudaSuccess;
-  k_energy<<<dim3(max_slices, nrep), 256, 0, s>>>(A, rep_ids, slice_base, nrep);
-  return cudaGetLastError();
+  // the batch on grid y, at most 65535 replicas per launch (the launches run
+  // in stream order, so the per-replica slice counters are reused safely)
+  for (int y0 = 0; y0 < nrep; y0 += 65535) {
+    const int ny = nrep - y0 < 65535 ? nrep - y0 : 65535;
+    k_energy<<<dim3(max_slices, ny), 256, 0, s>>>(A, rep_ids + y0, slice_base + y0, ny);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_observables(const DevArrays& A, const int* rep_ids, int nrep, cudaStream_t s) {
