@@ -1,7 +1,7 @@
 """GPU parity: the CUDA path (through the C ABI) against the CPU oracle and
 the reference's golden vectors.
 
-Tolerances (the benchmark spec): pair lists bit-exact as integer sets;
+Tolerances: pair lists bit-exact as integer sets;
 per-step forces and energies within 1e-5 relative (forces normwise over all
 beads: |F_gpu - F_ref|_2 / |F_ref|_2); 1,000-step noise-off trajectories
 within 1e-4 A RMSD.
