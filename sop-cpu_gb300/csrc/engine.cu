@@ -204,46 +204,11 @@ static cudaError_t dalloc(T** p, size_t n) {
   return cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
 }
 
-extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** out) {
-  if (!out) return SOP_ERR_ARG;
-  *out = nullptr;
-  sop_engine_config cfg;
-  sop_engine_config_default(&cfg);
-  if (cfg_in) {
-    cfg.device = cfg_in->device;
-    if (cfg_in->max_beads > 0) cfg.max_beads = cfg_in->max_beads;
-    if (cfg_in->max_replicas > 0) cfg.max_replicas = cfg_in->max_replicas;
-    if (cfg_in->max_list_entries > 0) cfg.max_list_entries = cfg_in->max_list_entries;
-    if (cfg_in->block_threads > 0) cfg.block_threads = cfg_in->block_threads;
-    if (cfg_in->lanes_per_bead > 0) cfg.lanes_per_bead = cfg_in->lanes_per_bead;
-    if (cfg_in->graph_steps > 0) cfg.graph_steps = cfg_in->graph_steps;
-    if (cfg_in->stage_limit != 0) cfg.stage_limit = cfg_in->stage_limit;
-    if (cfg_in->chunk_beads > 0) cfg.chunk_beads = cfg_in->chunk_beads;
-    if (cfg_in->build_slice_beads > 0) cfg.build_slice_beads = cfg_in->build_slice_beads;
-    if (cfg_in->step_min_blocks > 0) cfg.step_min_blocks = cfg_in->step_min_blocks;
-    if (cfg_in->step_strategy > 0) cfg.step_strategy = cfg_in->step_strategy;
-    if (cfg_in->group_rebuild_pct != 0) cfg.group_rebuild_pct = cfg_in->group_rebuild_pct;
-    cfg.lean_prep = cfg_in->lean_prep < 0 ? -1 : 0;
-  }
-  if (cfg.group_rebuild_pct < 0 || cfg.group_rebuild_pct >= 100) cfg.group_rebuild_pct = 0;
-  if (cfg.step_strategy != 1) cfg.step_strategy = 0;
-  if (cfg.step_min_blocks < 2 || cfg.step_min_blocks > 4) cfg.step_min_blocks = 3;
-  if (cfg.step_strategy == 1 && cfg.step_min_blocks == 4) cfg.step_min_blocks = 3;
-  if (cfg.stage_limit > kStageMax) cfg.stage_limit = kStageMax;
-  if (cfg.chunk_beads < 32) cfg.chunk_beads = 32;
-  if (cfg.build_slice_beads < kMinSliceBeads) cfg.build_slice_beads = kMinSliceBeads;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
-    cudaGetLastError();
-    return SOP_ERR_NODEV;
-  }
-  if (cfg.device < 0 || cfg.device >= ndev) return SOP_ERR_ARG;
-  int lanes = cfg.lanes_per_bead;
-  if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16) return SOP_ERR_ARG;
-  if (cfg.block_threads % 32 || cfg.block_threads < 64 || cfg.block_threads > 256) return SOP_ERR_ARG;
-  std::unique_ptr<sop_engine> e(new (std::nothrow) sop_engine());
-  if (!e) return SOP_ERR_NOMEM;
-  e->cfg = cfg;
+// Device and host resources of a new engine (e->cfg already validated).  On
+// failure the caller destroys the partly built engine, which frees what was
+// made (every pointer starts null).
+static int engine_init(sop_engine* e) {
+  const sop_engine_config& cfg = e->cfg;
   CK(cudaSetDevice(cfg.device));
   CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
   CK(cudaGetDeviceProperties(&e->prop, cfg.device));
@@ -360,6 +325,54 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   e->pro_grid = 2 * e->prop.multiProcessorCount;  // k_prep CTAs (two per SM, all resident)
   for (int k = 0; k < 4; k++) CK(cudaEventCreate(&e->ev[k]));
   CK(cudaStreamSynchronize(e->stream));
+  return SOP_OK;
+}
+
+extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** out) {
+  if (!out) return SOP_ERR_ARG;
+  *out = nullptr;
+  sop_engine_config cfg;
+  sop_engine_config_default(&cfg);
+  if (cfg_in) {
+    cfg.device = cfg_in->device;
+    if (cfg_in->max_beads > 0) cfg.max_beads = cfg_in->max_beads;
+    if (cfg_in->max_replicas > 0) cfg.max_replicas = cfg_in->max_replicas;
+    if (cfg_in->max_list_entries > 0) cfg.max_list_entries = cfg_in->max_list_entries;
+    if (cfg_in->block_threads > 0) cfg.block_threads = cfg_in->block_threads;
+    if (cfg_in->lanes_per_bead > 0) cfg.lanes_per_bead = cfg_in->lanes_per_bead;
+    if (cfg_in->graph_steps > 0) cfg.graph_steps = cfg_in->graph_steps;
+    if (cfg_in->stage_limit != 0) cfg.stage_limit = cfg_in->stage_limit;
+    if (cfg_in->chunk_beads > 0) cfg.chunk_beads = cfg_in->chunk_beads;
+    if (cfg_in->build_slice_beads > 0) cfg.build_slice_beads = cfg_in->build_slice_beads;
+    if (cfg_in->step_min_blocks > 0) cfg.step_min_blocks = cfg_in->step_min_blocks;
+    if (cfg_in->step_strategy > 0) cfg.step_strategy = cfg_in->step_strategy;
+    if (cfg_in->group_rebuild_pct != 0) cfg.group_rebuild_pct = cfg_in->group_rebuild_pct;
+    cfg.lean_prep = cfg_in->lean_prep < 0 ? -1 : 0;
+  }
+  if (cfg.group_rebuild_pct < 0 || cfg.group_rebuild_pct >= 100) cfg.group_rebuild_pct = 0;
+  if (cfg.step_strategy != 1) cfg.step_strategy = 0;
+  if (cfg.step_min_blocks < 2 || cfg.step_min_blocks > 4) cfg.step_min_blocks = 3;
+  if (cfg.step_strategy == 1 && cfg.step_min_blocks == 4) cfg.step_min_blocks = 3;
+  if (cfg.stage_limit > kStageMax) cfg.stage_limit = kStageMax;
+  if (cfg.chunk_beads < 32) cfg.chunk_beads = 32;
+  if (cfg.build_slice_beads < kMinSliceBeads) cfg.build_slice_beads = kMinSliceBeads;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    cudaGetLastError();
+    return SOP_ERR_NODEV;
+  }
+  if (cfg.device < 0 || cfg.device >= ndev) return SOP_ERR_ARG;
+  int lanes = cfg.lanes_per_bead;
+  if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16) return SOP_ERR_ARG;
+  if (cfg.block_threads % 32 || cfg.block_threads < 64 || cfg.block_threads > 256) return SOP_ERR_ARG;
+  std::unique_ptr<sop_engine> e(new (std::nothrow) sop_engine());
+  if (!e) return SOP_ERR_NOMEM;
+  e->cfg = cfg;
+  const int rc = engine_init(e.get());
+  if (rc != SOP_OK) {
+    sop_engine_destroy(e.release());  // frees whatever was made before the failure
+    return rc;
+  }
   *out = e.release();
   return SOP_OK;
 }
