@@ -155,11 +155,19 @@ def test_port_cell_list_matches_golden(path):
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
 def test_port_steepest_descent_matches_reference_program(path):
-    """sop.x at T=0 (v stays 0, x += a2 F, sop.cpp:316) against update.out."""
+    """sop.x at T=0 (v stays 0, x += a2 F, sop.cpp:316) against update.out,
+    and the positions at the start and at every output step against the
+    frames it appended to traj.bin / traj_uncorrected.bin (io.cpp:280-303)."""
     g = np.load(path)
+    n = len(g["xyz"])
+    frames = g["sd_traj"].reshape(-1, n, 3)
+    frames_unc = g["sd_traj_unc"].reshape(-1, n, 3)
+    assert len(frames) == len(frames_unc) == 1 + len(g["sd_update"])
     port = port_for(system_from_golden(g), golden_script(temp="0.0"))
     port.setup(True)
-    for row in g["sd_update"]:
+    np.testing.assert_allclose(port.coords(0), frames[0], rtol=0, atol=1e-6)  # %f columns
+    np.testing.assert_allclose(port.coords(1), frames_unc[0], rtol=0, atol=1e-6)
+    for k, row in enumerate(g["sd_update"]):
         step = int(row[0])
         port.run(step - int(port.param("force_evals")) + 1)
         port.energy_eval()
@@ -168,6 +176,8 @@ def test_port_steepest_descent_matches_reference_program(path):
                port.energy("e_vdw_rr"), port.energy("rna_etot"), port.energy("Q"),
                port.count("contct_nat"), port.energy("rgsq")]
         np.testing.assert_allclose(got, row[2:], rtol=0, atol=2e-6)  # %f columns
+        np.testing.assert_allclose(port.coords(0), frames[k + 1], rtol=0, atol=1e-6)
+        np.testing.assert_allclose(port.coords(1), frames_unc[k + 1], rtol=0, atol=1e-6)
     np.testing.assert_allclose(port.coords(1), g["sd_unc"], rtol=0, atol=2e-6)
 
 
