@@ -110,11 +110,19 @@ def job_totals(units, seconds, world, device="cpu"):
     return float(u.item()), float(t.item())
 
 
-def build_workload(args, rank):
-    """Each rank its own seeded mix (replicas only: no data is shared)."""
+def build_workload(args, rank, synth_many=None):
+    """Each rank its own seeded mix (replicas only: no data is shared).
+    ``synth_many`` swaps the engine library's generator for the stand-alone
+    build of the same source (the reference arm loads no engine code)."""
     from sop_gb300 import systems as S
-    systems, temps = S.mixed_batch(args.replicas, args.lo, args.hi, seed=2000 + 100000 * rank)
+    systems, temps = S.mixed_batch(args.replicas, args.lo, args.hi, seed=2000 + 100000 * rank,
+                                   synth_many=synth_many)
     return systems, temps
+
+
+def workload_name(args, systems):
+    return ("batched replicas: %d chains, N log-uniform %d-%d (%d beads), T 0.4-0.9, zeta 50, "
+            "dt 0.05" % (len(systems), args.lo, args.hi, sum(s.nbead for s in systems)))
 
 
 def default_workload(args):
@@ -524,8 +532,7 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair forces / f64 state",
         "data": "synthetic (seeded chains)",
-        "config": {"workload": "batched replicas: %d chains, N log-uniform %d-%d (%d beads), "
-                               "T 0.4-0.9, zeta 50, dt 0.05" % (len(systems), args.lo, args.hi, beads),
+        "config": {"workload": workload_name(args, systems),
                    "md_steps_per_step": md, "list_mode": args.list_mode, "skin": args.skin,
                    "autotuned": tuned,
                    "parallelism": "replicas" if world > 1 else "single GPU",
@@ -559,7 +566,8 @@ def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    systems, temps = build_workload(args, 0)
+    from oracle import oracle as O
+    systems, temps = build_workload(args, 0, synth_many=O.synth_many)
     threads = os.cpu_count() or 1
     per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
     vals = []
@@ -572,8 +580,7 @@ def run_reference(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded chains)", "impl": "reference",
-        "config": {"workload": "batched replicas: %d chains, N log-uniform %d-%d, T 0.4-0.9, "
-                               "zeta 50, dt 0.05" % (len(systems), args.lo, args.hi)},
+        "config": {"workload": workload_name(args, systems)},
         "cpu_baseline": dict(cb, value=value),
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

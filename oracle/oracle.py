@@ -3,6 +3,9 @@
 ``Port``  -- oracle/sop_oracle.c, the C restatement (builds on any host).
 ``Ref``   -- oracle/_ref/libsopref.so, the unmodified SOP-CPU sources behind
              oracle/ref_harness.cpp (built only where the reference tree is).
+``synth_chain`` / ``synth_many`` -- oracle/_build/libsopsynth.so, the seeded
+             workload generator built on its own (host code only), so a CPU
+             baseline builds its inputs without loading the engine library.
 
 Both expose the same methods so a test can run one script through either.
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
@@ -19,6 +22,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libsoporacle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libsopref.so")
 REF_EXE = os.path.join(HERE, "_ref", "sop.x")
+REF_TREE_FILE = os.path.join(HERE, "_ref", "ref_tree")
+SYNTH_LIB = os.path.join(HERE, "_build", "libsopsynth.so")
 DP = C.POINTER(C.c_double)
 IP = C.POINTER(C.c_int)
 
@@ -41,6 +46,9 @@ def _port_lib():
         L.sopo_set_topology_pruned.argtypes = [
             C.c_void_p, C.c_int, IP, IP, C.c_int, IP, IP, DP, C.c_int, IP, IP, IP,
             C.c_int, IP, IP, DP, DP, C.c_double]
+        L.sopo_set_topology.argtypes = [
+            C.c_void_p, C.c_int, C.c_int, IP, IP, DP, C.c_int, IP, IP, IP,
+            C.c_int, IP, IP, DP, IP, IP]
         L.sopo_set_coords.argtypes = [C.c_void_p, C.c_int, DP]
         L.sopo_get_coords.argtypes = [C.c_void_p, C.c_int, DP]
         L.sopo_set_param.argtypes = [C.c_void_p, C.c_char_p, C.c_double]
@@ -89,6 +97,48 @@ def ref_available() -> bool:
     return os.path.exists(REF_LIB)
 
 
+def ref_tree():
+    """The reference source tree oracle/_ref was built from, or None."""
+    try:
+        with open(REF_TREE_FILE) as f:
+            path = f.read().strip()
+        return path if os.path.isdir(path) else None
+    except OSError:
+        return None
+
+
+_synth = None
+
+
+def _synth_lib():
+    global _synth
+    if _synth is None:
+        if not os.path.exists(SYNTH_LIB):
+            raise RuntimeError("workload generator not built: make -C oracle synth")
+        L = C.CDLL(SYNTH_LIB)
+        L.sop_synth_chain.argtypes = [C.c_uint64, C.c_int, C.c_int, DP]
+        L.sop_synth_globule.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int, DP]
+        _synth = L
+    return _synth
+
+
+def synth_chain(seed, nbead, compact_steps=2000):
+    """The seeded compact chain of sop_synth_chain, from the stand-alone build."""
+    out = np.zeros((nbead, 3), np.float64)
+    rc = _synth_lib().sop_synth_chain(C.c_uint64(seed), nbead, compact_steps, out.ctypes.data_as(DP))
+    if rc != 0:
+        raise RuntimeError("sop_synth_chain = %d" % rc)
+    return out
+
+
+def synth_many(jobs, compact_steps=2000, workers=None):
+    """[(seed, nbead)] -> list of (nbead,3) arrays on host threads."""
+    from concurrent.futures import ThreadPoolExecutor
+    workers = workers or min(32, os.cpu_count() or 1)
+    with ThreadPoolExecutor(workers) as ex:
+        return list(ex.map(lambda j: synth_chain(j[0], j[1], compact_steps), jobs))
+
+
 ENERGY_NAMES = ("e_bnd", "e_ang_ss", "e_vdw_rr", "e_vdw_rr_att", "e_vdw_rr_rep", "rna_etot")
 
 
@@ -118,7 +168,12 @@ class Port:
     def set_system(self, system, prune=None):
         """Implicit-candidate topology from a sop_gb300.systems.System; with
         `prune` (A), only the pairs closer than that at the system's positions
-        plus the natives (sopo_set_topology_pruned, for large systems)."""
+        plus the natives (sopo_set_topology_pruned, for large systems).  A
+        system with exclusions goes in as the explicit candidate list a vdw
+        file would hold (sopo_set_topology: natives and the non-natives the
+        file lists, lexicographic order, each with its bead types)."""
+        if system.exclusions is not None and prune is None:
+            return self._set_explicit(system)
         n = system.nbead
         ib, jb, r0 = [np.ascontiguousarray(a) for a in system.bonds]
         ia, ja, ka, _ = [np.ascontiguousarray(a) for a in system.angles]
@@ -144,6 +199,39 @@ class Port:
                                                  float(prune))
         if rc != 0:
             raise RuntimeError("sopo_set_topology = %d" % rc)
+        self.set_coords(0, xyz)
+        self.set_coords(1, xyz)
+
+    def _set_explicit(self, system):
+        from sop_gb300 import systems as S  # candidate enumeration only
+        n = system.nbead
+        ib, jb, r0 = [np.ascontiguousarray(a) for a in system.bonds]
+        ia, ja, ka, _ = [np.ascontiguousarray(a) for a in system.angles]
+        in_, jn, rn = [np.asarray(a) for a in system.natives]
+        ib, jb, ia, ja, ka = [a.astype(np.int32) for a in (ib, jb, ia, ja, ka)]
+        r0 = r0.astype(np.float64)
+        typ = (np.ones(n, np.int32) if system.bead_type is None
+               else np.asarray(system.bead_type, np.int32))
+        ri, rj = S.candidate_pairs(system)
+        ic = np.concatenate([np.asarray(in_, np.int64), ri.astype(np.int64)])
+        jc = np.concatenate([np.asarray(jn, np.int64), rj.astype(np.int64)])
+        # non-natives carry a distance at or above rcut_nat of their types
+        rc = np.concatenate([np.asarray(rn, np.float64),
+                             S.RCUT_NAT[typ[ri], typ[rj]] + 1.0])
+        order = np.lexsort((jc, ic))
+        ic = np.ascontiguousarray(ic[order], np.int32)
+        jc = np.ascontiguousarray(jc[order], np.int32)
+        rc = np.ascontiguousarray(rc[order])
+        ti = np.ascontiguousarray(typ[ic], np.int32)
+        tj = np.ascontiguousarray(typ[jc], np.int32)
+        ip = lambda a: a.ctypes.data_as(IP)
+        dp = lambda a: a.ctypes.data_as(DP)
+        xyz = np.ascontiguousarray(system.xyz, np.float64)
+        self._keep = (ib, jb, r0, ia, ja, ka, ic, jc, rc, ti, tj, xyz)
+        rc_ = self.L.sopo_set_topology(self.h, n, len(ib), ip(ib), ip(jb), dp(r0), len(ia), ip(ia),
+                                       ip(ja), ip(ka), len(ic), ip(ic), ip(jc), dp(rc), ip(ti), ip(tj))
+        if rc_ != 0:
+            raise RuntimeError("sopo_set_topology = %d" % rc_)
         self.set_coords(0, xyz)
         self.set_coords(1, xyz)
 

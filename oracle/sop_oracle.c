@@ -45,6 +45,9 @@ struct sopo_sys {
   uint64_t seed;
   uint64_t force_evals; /* noise counter: one per force_eval */
   int force_on[4];      /* random, fene, angle, vdw */
+  /* constant pulling force on two beads (no reference term) */
+  double pull_f;        /* kcal/mol/A; 0 = off */
+  int pull_i, pull_j;   /* pulled beads; pull_j < 0 = the last bead */
   int inlup;
   /* energies / observables */
   double e_bnd, e_ang_ss, e_vdw_att, e_vdw_rep, e_vdw, etot;
@@ -104,6 +107,9 @@ sopo_sys* sopo_create(void) {
   /* global.cpp:200-202: random, bonds, angles, vdw on */
   s->force_on[0] = s->force_on[1] = s->force_on[2] = s->force_on[3] = 1;
   s->inlup = 1;
+  s->pull_f = 0.0;
+  s->pull_i = 0;
+  s->pull_j = -1;
   return s;
 }
 
@@ -460,6 +466,9 @@ int sopo_set_param(sopo_sys* s, const char* name, double v) {
   else if (!strcmp(name, "neighborlist")) s->neighborlist = (int)v;
   else if (!strcmp(name, "celllist")) s->celllist = (int)v;
   else if (!strcmp(name, "force_evals")) s->force_evals = (uint64_t)v;
+  else if (!strcmp(name, "pull_force")) s->pull_f = v;
+  else if (!strcmp(name, "pull_i")) s->pull_i = (int)v;
+  else if (!strcmp(name, "pull_j")) s->pull_j = (int)v;
   else return -1;
   return 0;
 }
@@ -488,6 +497,9 @@ double sopo_get_param(const sopo_sys* s, const char* name) {
   if (!strcmp(name, "k_bnd")) return s->k_bnd;
   if (!strcmp(name, "R0")) return s->R0;
   if (!strcmp(name, "force_evals")) return (double)s->force_evals;
+  if (!strcmp(name, "pull_force")) return s->pull_f;
+  if (!strcmp(name, "pull_i")) return s->pull_i;
+  if (!strcmp(name, "pull_j")) return s->pull_j;
   return NAN;
 }
 
@@ -906,13 +918,33 @@ static void vdw_forces(sopo_sys* s) {
   }
 }
 
-/* energy.cpp:21-45 with the term order of set_forces (energy.cpp:78-113). */
+/* Constant-force pulling of two beads apart along their separation, the
+ * served workload's optional term.  The reference has no such term (its
+ * tension switch is off by default, global.cpp:200, and has no force
+ * routine), so this restates the engine's definition: with u = x_j - x_i
+ * (unwrapped positions, no minimum image), bead i gets -f u/|u| and bead j
+ * +f u/|u|, f in kcal/mol/A (1 pN = 1/69.48 kcal/mol/A).  Independent of the
+ * force-term switches; applied after them. */
+static void pull_force(sopo_sys* s) {
+  const int i = s->pull_i, j = s->pull_j < 0 ? s->nbead - 1 : s->pull_j;
+  if (i < 0 || i >= s->nbead || j < 0 || j >= s->nbead || i == j) return;
+  const double* u = s->unc_pos;
+  double ux = u[3 * j] - u[3 * i], uy = u[3 * j + 1] - u[3 * i + 1], uz = u[3 * j + 2] - u[3 * i + 2];
+  double d = sqrt(ux * ux + uy * uy + uz * uz);
+  double fx = s->pull_f * ux / d, fy = s->pull_f * uy / d, fz = s->pull_f * uz / d;
+  s->force[3 * i] -= fx; s->force[3 * i + 1] -= fy; s->force[3 * i + 2] -= fz;
+  s->force[3 * j] += fx; s->force[3 * j + 1] += fy; s->force[3 * j + 2] += fz;
+}
+
+/* energy.cpp:21-45 with the term order of set_forces (energy.cpp:78-113),
+ * then the pulling term when one is set. */
 void sopo_force_eval(sopo_sys* s) {
   clear_forces(s);
   if (s->force_on[0]) random_force(s);
   if (s->force_on[1]) fene_forces(s);
   if (s->force_on[2]) soft_sphere_angular_forces(s);
   if (s->force_on[3]) vdw_forces(s);
+  if (s->pull_f != 0.0) pull_force(s);
   s->force_evals++;
 }
 

@@ -66,7 +66,8 @@ int sopo_set_coords(sopo_sys* s, int which, const double* xyz);
 int sopo_get_coords(const sopo_sys* s, int which, double* xyz);
 
 /* Scalars by name: T, zeta, h, halfh, a1..a5, boxl, ncell, lcell, nstep, nup,
- * nnlup, run, seed, neighborlist, celllist, sim_type, k_bnd, R0.
+ * nnlup, run, seed, neighborlist, celllist, sim_type, k_bnd, R0, and the
+ * pulling term pull_force (kcal/mol/A, 0 = off), pull_i, pull_j (<0: last).
  * "zeta"/"t_step"/"dynamics" follow the set-command side effects (params.cpp:
  * 84-98) only through sopo_set_command(). */
 int sopo_set_param(sopo_sys* s, const char* name, double v);

@@ -75,7 +75,12 @@ class _Desc:
         in_, jn, rn = system.natives
         d.nnat = len(in_)
         d.in_, d.jn, d.rn = L.iptr(iarr(in_)), L.iptr(iarr(jn)), L.dptr(darr(rn))
-        d.nexcl = 0
+        if system.exclusions is not None and len(system.exclusions[0]):
+            ie, je = system.exclusions
+            d.nexcl = len(ie)
+            d.ie, d.je = L.iptr(iarr(ie)), L.iptr(iarr(je))
+        else:
+            d.nexcl = 0
         d.params = params
         self.desc = d
 

@@ -5,7 +5,9 @@ A :class:`System` holds what SOP-CPU loads from its four input files
 list ``i j r type_i type_j`` (native iff ``r < rcut_nat``, params.cpp:197) and
 the initial coordinates.  Non-native candidates are implicit: every pair on
 different chains, or on one chain with ``|i-j| > 2``, that is not native --
-exactly the set a vdw file listing all such pairs describes.
+exactly the set a vdw file listing all such pairs describes -- minus the
+``exclusions``: pairs of that set a vdw file does not list, which therefore
+never interact (params.cpp:186-232).
 
 Values are rounded to the 6 decimals the files carry, so the engine, the
 oracle and the reference program read identical doubles.
@@ -21,6 +23,8 @@ import numpy as np
 from . import _lib
 
 RCUT_NAT_11 = 8.0  # global.cpp:90 (type 1-1)
+# rcut_nat[ti][tj] (global.cpp:89-91): a vdw candidate is native iff r < this
+RCUT_NAT = np.array([[0.0, 0.0, 0.0], [0.0, 8.0, 11.0], [0.0, 11.0, 14.0]])
 
 
 def _r6(a):
@@ -38,6 +42,8 @@ class System:
     bead_type: np.ndarray = None    # (N,) int, default 1
     chain: np.ndarray = None        # (N,) int, default 0
     params: dict = field(default_factory=dict)  # reference "set" keywords
+    exclusions: tuple = None        # (ie, je) 0-based, i<j: implicit candidates
+                                    # the vdw file leaves out (never interact)
 
     @property
     def nbead(self) -> int:
@@ -55,16 +61,19 @@ class System:
         return total - same_close
 
 
-def native_pairs(xyz: np.ndarray, chain=None, cutoff: float = RCUT_NAT_11, min_sep: int = 3):
+def native_pairs(xyz: np.ndarray, chain=None, cutoff: float = RCUT_NAT_11, min_sep: int = 3,
+                 bead_type=None):
     """Pairs (i<j) closer than ``cutoff`` in the native structure, with
-    ``|i-j| >= min_sep`` on one chain (natives are intra-chain only)."""
+    ``|i-j| >= min_sep`` on one chain (natives are intra-chain only).  With
+    ``bead_type`` the cutoff of each pair is rcut_nat[ti][tj] instead."""
     n = xyz.shape[0]
+    search = cutoff if bead_type is None else float(RCUT_NAT.max())
     try:
         from scipy.spatial import cKDTree
-        pairs = np.array(sorted(cKDTree(xyz).query_pairs(cutoff + 1e-3)), dtype=np.int64)
+        pairs = np.array(sorted(cKDTree(xyz).query_pairs(search + 1e-3)), dtype=np.int64)
     except ImportError:  # pragma: no cover - scipy is in both images
         d = np.sqrt(((xyz[:, None, :] - xyz[None, :, :]) ** 2).sum(-1))
-        ii, jj = np.nonzero(np.triu(d < cutoff + 1e-3, 1))
+        ii, jj = np.nonzero(np.triu(d < search + 1e-3, 1))
         pairs = np.stack([ii, jj], 1)
     if pairs.size == 0:
         return (np.zeros(0, np.int32),) * 2 + (np.zeros(0),)
@@ -73,14 +82,20 @@ def native_pairs(xyz: np.ndarray, chain=None, cutoff: float = RCUT_NAT_11, min_s
     keep = same & (j - i >= min_sep)
     i, j = i[keep], j[keep]
     r = _r6(np.sqrt(((xyz[j] - xyz[i]) ** 2).sum(1)))
-    keep = r < cutoff
+    if bead_type is None:
+        keep = r < cutoff
+    else:
+        t = np.asarray(bead_type, np.int64)
+        keep = r < RCUT_NAT[t[i], t[j]]
     order = np.lexsort((j[keep], i[keep]))
     return (i[keep][order].astype(np.int32), j[keep][order].astype(np.int32), r[keep][order])
 
 
-def system_from_xyz(xyz: np.ndarray, chain=None, params: dict | None = None) -> System:
+def system_from_xyz(xyz: np.ndarray, chain=None, params: dict | None = None,
+                    bead_type=None) -> System:
     """Topology of the SOP model at a native structure: bonds i,i+1 and angles
-    i,i+1,i+2 within each chain, natives within 8 A at |i-j|>2."""
+    i,i+1,i+2 within each chain, natives at |i-j|>2 within rcut_nat of the
+    pair's bead types (8 A for type 1-1, 11 A for 1-2, 14 A for 2-2)."""
     xyz = _r6(xyz)
     n = xyz.shape[0]
     ch = np.zeros(n, np.int32) if chain is None else np.asarray(chain, np.int32)
@@ -90,10 +105,51 @@ def system_from_xyz(xyz: np.ndarray, chain=None, params: dict | None = None) -> 
     ia = np.array([i for i in range(n - 2) if ch[i] == ch[i + 2]], np.int32)
     ja, ka = ia + 1, ia + 2
     a0 = _r6(np.sqrt(((xyz[ka] - xyz[ia]) ** 2).sum(1)))
-    nat = native_pairs(xyz, None if chain is None else ch)
+    typ = np.ones(n, np.int32) if bead_type is None else np.asarray(bead_type, np.int32)
+    if typ.shape != (n,) or not np.all((typ == 1) | (typ == 2)):
+        raise ValueError("bead types must be 1 or 2, one per bead")
+    nat = native_pairs(xyz, None if chain is None else ch,
+                       bead_type=None if bead_type is None else typ)
     return System(xyz=xyz, bonds=(ib, jb, r0), angles=(ia, ja, ka, a0), natives=nat,
-                  bead_type=np.ones(n, np.int32), chain=None if chain is None else ch,
+                  bead_type=typ, chain=None if chain is None else ch,
                   params=dict(params or {}))
+
+
+def candidate_pairs(system: System):
+    """The non-native candidates (i<j, lexicographic order) a vdw file
+    listing them explicitly would hold: the implicit set minus the natives
+    and the exclusions."""
+    n = system.nbead
+    ii, jj = np.triu_indices(n, 1)
+    if system.chain is None:
+        keep = jj - ii > 2
+    else:
+        ch = np.asarray(system.chain)
+        keep = (ch[ii] != ch[jj]) | (jj - ii > 2)
+    ii, jj = ii[keep], jj[keep]
+    drop = set()
+    in_, jn, _ = system.natives
+    drop.update(zip(np.asarray(in_).tolist(), np.asarray(jn).tolist()))
+    if system.exclusions is not None:
+        drop.update(zip(np.asarray(system.exclusions[0]).tolist(),
+                        np.asarray(system.exclusions[1]).tolist()))
+    if drop:
+        key = ii.astype(np.int64) * n + jj
+        gone = np.array([a * n + b for a, b in drop], np.int64)
+        keep = ~np.isin(key, gone)
+        ii, jj = ii[keep], jj[keep]
+    return ii.astype(np.int32), jj.astype(np.int32)
+
+
+def with_exclusions(system: System, fraction: float, seed: int) -> System:
+    """A copy of ``system`` whose vdw file leaves out a seeded ``fraction`` of
+    the non-native candidates (those pairs then never interact)."""
+    ii, jj = candidate_pairs(system)
+    rng = np.random.default_rng(seed)
+    pick = np.sort(rng.choice(len(ii), int(round(fraction * len(ii))), replace=False))
+    out = System(**{k: getattr(system, k) for k in system.__dataclass_fields__})
+    out.exclusions = (ii[pick].astype(np.int32), jj[pick].astype(np.int32))
+    return out
 
 
 def synth_chain(seed: int, nbead: int, compact_steps: int = 2000, params=None) -> System:
@@ -143,6 +199,10 @@ def write_reference_files(system: System, dirpath: str, script=None, run: bool =
             f.write("%d %d %d %.6f\n" % (a + 1, b + 1, c + 1, r))
     in_, jn, rn = system.natives
     nat = {(int(a), int(b)): float(r) for a, b, r in zip(in_, jn, rn)}
+    excl = set()
+    if system.exclusions is not None:
+        excl = set(zip(np.asarray(system.exclusions[0]).tolist(),
+                       np.asarray(system.exclusions[1]).tolist()))
     ch = system.chain
     types = system.bead_type if system.bead_type is not None else np.ones(n, np.int32)
     lines = []
@@ -155,7 +215,11 @@ def write_reference_files(system: System, dirpath: str, script=None, run: bool =
             if r is not None:
                 natt += 1
             else:
-                r = max(RCUT_NAT_11 + 1.0, float(np.sqrt(((system.xyz[j] - system.xyz[i]) ** 2).sum())))
+                if (i, j) in excl:
+                    continue  # left out of the file: never interacts
+                # any distance at or above rcut_nat keeps the pair non-native
+                r = max(RCUT_NAT[types[i], types[j]] + 1.0,
+                        float(np.sqrt(((system.xyz[j] - system.xyz[i]) ** 2).sum())))
             lines.append("%d %d %.6f %d %d\n" % (i + 1, j + 1, r, types[i], types[j]))
     with open(os.path.join(dirpath, "vdw.dat"), "w") as f:
         f.write("ncon_att %d ncon_rep %d\n" % (natt, len(lines) - natt))
@@ -248,12 +312,15 @@ def loguniform_sizes(seed: int, count: int, lo: int, hi: int) -> np.ndarray:
 
 
 def mixed_batch(count: int = 512, lo: int = 30, hi: int = 1500, seed: int = 2000,
-                compact_steps: int = 2000):
+                compact_steps: int = 2000, synth_many=None):
     """Batched-replica workload: ``count`` chains with log-uniform bead counts
     in [lo, hi] and temperatures uniform in [0.4, 0.9]; replica r is seeded
-    ``seed + r``.  Returns (systems, temperatures)."""
+    ``seed + r``.  Returns (systems, temperatures).  ``synth_many`` replaces
+    the engine library's generator with another build of the same source
+    (same seeds, same coordinates)."""
     sizes = loguniform_sizes(seed, count, lo, hi)
     temps = np.random.default_rng(seed + 7).uniform(0.4, 0.9, count)
-    xyzs = _lib.synth_many([(seed + r, int(n)) for r, n in enumerate(sizes)], compact_steps)
+    gen = synth_many or _lib.synth_many
+    xyzs = gen([(seed + r, int(n)) for r, n in enumerate(sizes)], compact_steps)
     systems = [system_from_xyz(x) for x in xyzs]
     return systems, temps

@@ -16,6 +16,13 @@ the reference's file formats, and stores inputs and outputs as .npz files:
   sd_unc      its final unccoord.out coordinates
   sd_traj*    its traj.bin / traj_uncorrected.bin frames (initial + every nup)
 
+sop_golden_N*.npz hold type-1 chains whose vdw file lists every candidate.
+sop_golden_types_N*.npz hold a chain with a seeded mix of bead types 1 and 2
+(sigma 3.8 / 5.4 / 7.0, rcut_nat 8 / 11 / 14 A, the type-dependent native
+coefficients: global.cpp:60-92) whose vdw file leaves out a seeded quarter of
+the non-native candidates (those pairs never interact, params.cpp:186-232);
+they add bead_type and the left-out pairs (ie, je, 0-based).
+
     make -C oracle ref && python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -36,7 +43,16 @@ from sop_gb300 import systems as S  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 SIZES = [(1030, 30), (1076, 76), (1150, 150)]
+TYPED = [(1250, 150)]
 NSTEPS = 100
+
+
+def typed_system(seed, n):
+    """A chain with a seeded mix of bead types (about 40% type 2) whose vdw
+    file leaves out a seeded quarter of the non-native candidates."""
+    xyz = S._lib.synth_chain(seed, n)
+    types = np.where(np.random.default_rng(seed + 1).random(n) < 0.4, 2, 1).astype(np.int32)
+    return S.with_exclusions(S.system_from_xyz(xyz, bead_type=types), 0.25, seed + 2)
 
 
 def script(mode="neighborlist", temp="0.6", nstep=NSTEPS, nup=50):
@@ -54,11 +70,13 @@ def lists(ref):
     return out
 
 
-def one(seed, n):
-    system = S.synth_chain(seed, n)
+def one(seed, n, typed=False):
+    system = typed_system(seed, n) if typed else S.synth_chain(seed, n)
     rec = dict(xyz=system.xyz, ib=system.bonds[0], jb=system.bonds[1], r0=system.bonds[2],
                ia=system.angles[0], ja=system.angles[1], ka=system.angles[2], a0=system.angles[3],
                in_=system.natives[0], jn=system.natives[1], rn=system.natives[2])
+    if typed:
+        rec.update(bead_type=system.bead_type, ie=system.exclusions[0], je=system.exclusions[1])
     ref = Ref()
     with tempfile.TemporaryDirectory() as d:
         path = S.write_reference_files(system, d, script(), run=False)
@@ -104,10 +122,13 @@ def one(seed, n):
         # record_traj's text frames (io.cpp:280-303): the start, then one per nup
         rec["sd_traj"] = np.loadtxt(os.path.join(d, "traj.bin"))
         rec["sd_traj_unc"] = np.loadtxt(os.path.join(d, "traj_uncorrected.bin"))
-    np.savez_compressed(os.path.join(OUT, "sop_golden_N%d.npz" % n), **rec)
-    print("wrote N=%d" % n)
+    name = ("sop_golden_types_N%d.npz" if typed else "sop_golden_N%d.npz") % n
+    np.savez_compressed(os.path.join(OUT, name), **rec)
+    print("wrote", name)
 
 
 if __name__ == "__main__":
     for seed, n in SIZES:
         one(seed, n)
+    for seed, n in TYPED:
+        one(seed, n, typed=True)

@@ -116,3 +116,36 @@ def test_fp64_replica_in_mixed_batch(eng):
         assert eng.status(r)[0] == 0
     for r in ids:
         eng.remove(r)
+
+
+def typed_chain(seed, n, frac):
+    xyz = L.synth_chain(seed, n)
+    types = np.where(np.random.default_rng(seed + 1).random(n) < 0.4, 2, 1).astype(np.int32)
+    return S.with_exclusions(S.system_from_xyz(xyz, bead_type=types), frac, seed + 2)
+
+
+@pytest.mark.parametrize("n", [150, 600])
+def test_fp64_typed_partial_candidates(eng, n):
+    """Bead types 1/2 and a vdw file that leaves out a quarter of the
+    non-native candidates, FP64 mode: forces and energies within 1e-10, a
+    1,000-step noise-off trajectory within 1e-8 A, with the pulling term on."""
+    system = typed_chain(9400 + n, n, 0.25)
+    kw = dict(pull_force=0.2, pull_i=0, pull_j=-1)
+    r = eng.add(system, make_params(script(), force_terms=DET, precision=L.PREC_FP64, **kw))
+    try:
+        port = port_for(system, script())
+        for k, v in kw.items():
+            port.set_param(k, v)
+        port.setup(True)
+        assert rel(eng.force(r), port.coords(3)) < F64_TOL
+        e = eng.energy(r)
+        for k, name in enumerate(O.ENERGY_NAMES):
+            want = port.energy(name)
+            assert abs(e[k] - want) <= E64_TOL * max(abs(want), 1e-3), (name, e[k], want)
+        eng.run_plain(r, 1000)
+        port.run(1000)
+        assert rmsd(eng.state(r)[1], port.coords(1)) < RMSD64_TOL
+        for k in range(4):
+            np.testing.assert_array_equal(pairset(*eng.pairs(r, k)), pairset(*port.pairs(k)))
+    finally:
+        eng.remove(r)

@@ -19,6 +19,8 @@ from oracle import oracle as O
 from sop_gb300 import systems as S
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "sop_golden_N*.npz")))
+GOLDEN_TYPED = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden",
+                                             "sop_golden_types_N*.npz")))
 needs_ref = pytest.mark.skipif(not O.ref_available(), reason="reference tree not built here")
 
 
@@ -31,9 +33,21 @@ def golden_script(mode="neighborlist", temp="0.6", nstep=100, nup=50, dynamics=N
 
 
 def system_from_golden(g):
+    typed = "bead_type" in g.files
     return S.System(xyz=g["xyz"], bonds=(g["ib"], g["jb"], g["r0"]),
                     angles=(g["ia"], g["ja"], g["ka"], g["a0"]),
-                    natives=(g["in_"], g["jn"], g["rn"]), bead_type=np.ones(len(g["xyz"]), np.int32))
+                    natives=(g["in_"], g["jn"], g["rn"]),
+                    bead_type=g["bead_type"] if typed else np.ones(len(g["xyz"]), np.int32),
+                    exclusions=(g["ie"], g["je"]) if typed else None)
+
+
+def typed_chain(seed, n, frac=0.25):
+    """A chain with a seeded mix of bead types 1/2 whose vdw file leaves out
+    a seeded fraction of the non-native candidates."""
+    xyz = S._lib.synth_chain(seed, n)
+    types = np.where(np.random.default_rng(seed + 1).random(n) < 0.4, 2, 1).astype(np.int32)
+    system = S.system_from_xyz(xyz, bead_type=types)
+    return S.with_exclusions(system, frac, seed + 2) if frac > 0 else system
 
 
 def port_for(system, script):
@@ -95,6 +109,130 @@ def test_port_equals_reference(n, mode, dyn):
 
 
 @needs_ref
+@pytest.mark.parametrize("n,mode,frac", [(76, "neighborlist", 0.0), (120, "neighborlist", 0.25),
+                                         (150, "celllist", 0.4), (90, "none", 0.3)])
+def test_port_equals_reference_types_and_exclusions(n, mode, frac):
+    """Bead types 1 and 2 (sigma, rcut_nat and the type-dependent native
+    coefficients, global.cpp:60-92) and a vdw file that leaves out part of the
+    non-native candidates (params.cpp:186-232): the reference reading the
+    files, the restatement reading the same files, and the restatement given
+    the system directly (sopo_set_topology / sopo_set_topology_implicit) agree
+    bit for bit."""
+    system = typed_chain(6100 + n, n, frac)
+    # the reference keeps its globals between loads: reset the integrator
+    scr = golden_script(mode, dynamics="underdamped")
+    ref, port_files = O.Ref(), O.Port()
+    port_direct = port_for(system, scr)
+    with tempfile.TemporaryDirectory() as d:
+        path = S.write_reference_files(system, d, scr, run=False)
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            ref.load_script(path)
+            port_files.load_script(path)
+        finally:
+            os.chdir(cwd)
+    assert ref.count("ncon_att") == len(system.natives[0])
+    assert ref.count("ncon_rep") == len(S.candidate_pairs(system)[0])
+    ports = (port_files, port_direct)
+    for o in (ref,) + ports:
+        o.set_force_terms(0, 1, 1, 1)
+        o.setup(True)
+    for p in ports:
+        for k in range(4):
+            np.testing.assert_array_equal(pairs(ref, k), pairs(p, k))
+        np.testing.assert_array_equal(ref.energies(), p.energies())
+        np.testing.assert_array_equal(ref.coords(3), p.coords(3))
+    for terms in ((0, 1, 0, 0), (0, 0, 1, 0), (0, 0, 0, 1)):
+        for o in (ref,) + ports:
+            o.set_force_terms(*terms)
+            o.force_eval()
+        for p in ports:
+            np.testing.assert_array_equal(ref.coords(3), p.coords(3))
+    for o in (ref,) + ports:
+        o.set_force_terms(0, 1, 1, 1)
+        o.force_eval()
+        o.run(60)
+        o.energy_eval()
+        o.observables()
+    for p in ports:
+        for which in (1, 2):
+            np.testing.assert_array_equal(ref.coords(which), p.coords(which))
+        np.testing.assert_array_equal(ref.energies(), p.energies())
+        for k in ("Q", "rgsq", "kinT"):
+            assert ref.energy(k) == p.energy(k)
+        for k in range(4):
+            np.testing.assert_array_equal(pairs(ref, k), pairs(p, k))
+
+
+def test_typed_system_files_hold_what_the_system_says():
+    """write_reference_files of a typed system with exclusions: every
+    non-native line carries a distance at or above its pair's rcut_nat (so
+    it stays non-native), excluded pairs are absent, types are per bead."""
+    system = typed_chain(6200, 60, 0.3)
+    with tempfile.TemporaryDirectory() as d:
+        S.write_reference_files(system, d, golden_script(), run=False)
+        rows = np.loadtxt(os.path.join(d, "vdw.dat"), skiprows=1)
+    i, j = rows[:, 0].astype(int) - 1, rows[:, 1].astype(int) - 1
+    t = system.bead_type
+    np.testing.assert_array_equal(rows[:, 3], t[i])
+    np.testing.assert_array_equal(rows[:, 4], t[j])
+    native = rows[:, 2] < S.RCUT_NAT[t[i], t[j]]
+    assert native.sum() == len(system.natives[0])
+    listed = set(zip(i.tolist(), j.tolist()))
+    assert not listed & set(zip(system.exclusions[0].tolist(), system.exclusions[1].tolist()))
+    assert len(listed) == system.candidate_count() - len(system.exclusions[0])
+
+
+def test_pull_force_term():
+    """The pulling term (no reference counterpart): f along the separation of
+    the two pulled beads, pushing them apart, added after the other terms;
+    equal and opposite, so the force sum is unchanged."""
+    system = S.synth_chain(6300, 80)
+    scr = golden_script()
+    base = port_for(system, scr)
+    pulled = port_for(system, scr)
+    f = 10.0 / 69.48  # 10 pN
+    pulled.set_param("pull_force", f)
+    pulled.set_param("pull_i", 3)
+    pulled.set_param("pull_j", 70)
+    for p in (base, pulled):
+        p.set_force_terms(0, 1, 1, 1)
+        p.setup(True)
+    x = system.xyz
+    u = x[70] - x[3]
+    d = np.sqrt((u * u).sum())
+    want = base.coords(3).copy()
+    want[3] -= f * u / d
+    want[70] += f * u / d
+    np.testing.assert_allclose(pulled.coords(3), want, rtol=0, atol=1e-12)
+    assert abs(pulled.coords(3).sum(0) - base.coords(3).sum(0)).max() < 1e-10
+    # default pulled pair: the first and the last bead
+    ends = port_for(system, scr)
+    ends.set_param("pull_force", f)
+    ends.set_force_terms(0, 1, 1, 1)
+    ends.setup(True)
+    u = x[-1] - x[0]
+    want = base.coords(3).copy()
+    want[0] -= f * u / np.sqrt((u * u).sum())
+    want[-1] += f * u / np.sqrt((u * u).sum())
+    np.testing.assert_allclose(ends.coords(3), want, rtol=0, atol=1e-12)
+
+
+def test_standalone_generator_equals_engine_library_generator():
+    """The workload generator built on its own (oracle/_build/libsopsynth.so,
+    loaded by the benchmark's reference arm) and the engine library's copy
+    give the same coordinates for the same seeds."""
+    from sop_gb300 import _lib as L
+    try:
+        L.lib()
+    except Exception:
+        pytest.skip("engine library not built")
+    for seed, n in ((11, 30), (2000, 700), (2511, 1500)):
+        np.testing.assert_array_equal(O.synth_chain(seed, n), L.synth_chain(seed, n))
+
+
+@needs_ref
 def test_reference_files_round_trip():
     """The vdw file the generator writes splits into exactly the natives it holds."""
     system = S.synth_chain(77, 60)
@@ -112,7 +250,8 @@ def test_reference_files_round_trip():
     np.testing.assert_array_equal(ref.coords(1), system.xyz)
 
 
-@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+@pytest.mark.parametrize("path", GOLDEN + GOLDEN_TYPED,
+                         ids=[os.path.basename(p) for p in GOLDEN + GOLDEN_TYPED])
 def test_port_matches_golden(path):
     g = np.load(path)
     system = system_from_golden(g)
@@ -144,7 +283,8 @@ def test_port_matches_golden(path):
         np.testing.assert_array_equal(pairs(port, k), g["traj_" + name])
 
 
-@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+@pytest.mark.parametrize("path", GOLDEN + GOLDEN_TYPED,
+                         ids=[os.path.basename(p) for p in GOLDEN + GOLDEN_TYPED])
 def test_port_cell_list_matches_golden(path):
     g = np.load(path)
     port = port_for(system_from_golden(g), golden_script("celllist"))
@@ -153,7 +293,8 @@ def test_port_cell_list_matches_golden(path):
         np.testing.assert_array_equal(pairs(port, k), g["cell_" + name])
 
 
-@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+@pytest.mark.parametrize("path", GOLDEN + GOLDEN_TYPED,
+                         ids=[os.path.basename(p) for p in GOLDEN + GOLDEN_TYPED])
 def test_port_steepest_descent_matches_reference_program(path):
     """sop.x at T=0 (v stays 0, x += a2 F, sop.cpp:316) against update.out,
     and the positions at the start and at every output step against the

@@ -2,7 +2,9 @@
 script and data files in, the same update.out rows and coordinate files out.
 Against sop.x's own output for a T = 0 (steepest-descent) run, carried by the
 golden fixtures: rows within 1e-5 relative (2e-6 absolute, the printed
-precision), final coordinates and every trajectory frame within 1e-5 A."""
+precision), final coordinates and every trajectory frame within 1e-5 A.
+The fixtures include a chain of bead types 1 and 2 whose vdw file leaves out
+a quarter of the non-native candidates."""
 import glob
 import os
 import subprocess
@@ -15,7 +17,8 @@ from sop_gb300 import systems as S
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 EXE = os.path.join(ROOT, "sop-cpu_gb300", "lib", "sop_gpu.x")
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "sop_golden_N*.npz")))
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "sop_golden_N*.npz")) +
+                glob.glob(os.path.join(os.path.dirname(__file__), "golden", "sop_golden_types_N*.npz")))
 
 
 def golden_script(temp="0.0", nstep=100, nup=50):  # as tests/golden/make_golden.py
@@ -26,9 +29,14 @@ def golden_script(temp="0.0", nstep=100, nup=50):  # as tests/golden/make_golden
 
 
 def system_from_golden(g):
+    """The fixture's system; sop_golden_types_* add bead types 1/2 and the
+    candidates their vdw file leaves out."""
+    typed = "bead_type" in g.files
     return S.System(xyz=g["xyz"], bonds=(g["ib"], g["jb"], g["r0"]),
                     angles=(g["ia"], g["ja"], g["ka"], g["a0"]),
-                    natives=(g["in_"], g["jn"], g["rn"]), bead_type=np.ones(len(g["xyz"]), np.int32))
+                    natives=(g["in_"], g["jn"], g["rn"]),
+                    bead_type=g["bead_type"] if typed else np.ones(len(g["xyz"]), np.int32),
+                    exclusions=(g["ie"], g["je"]) if typed else None)
 
 
 def test_program_usage():
