@@ -340,24 +340,31 @@ int sop_synth_globule(uint64_t seed, int nchain, int chain_len, int compact_step
 /* ---- neighbor list without allocation ---------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory: hosts whose device memory belongs to their own pool, and loops that
- * cannot take the device-wide synchronization cudaMalloc / cudaFree may cause.  Every input and
- * output is a device pointer owned by the caller; the only other memory used
- * is a fixed static scratch array in the library (about 0.6 MB, held on each
- * GPU that loads the library until exit), sized for SOP_NOALLOC_MAX_BEADS.
- *   xyz      3*nbead doubles, x y z per bead (unc_pos)
- *   bead_type, chain   nbead ints each, or NULL (all type 1, one chain)
+ * cannot take the device-wide synchronization cudaMalloc / cudaFree may
+ * cause.  Every input and output is a device pointer owned by the caller; the
+ * only other memory used is a fixed static scratch array in the library
+ * (about 0.6 MB, held on each GPU that loads the library until exit), sized
+ * for SOP_NOALLOC_MAX_BEADS.
+ *   xyz      3*nbead doubles, x y z per bead (unc_pos), |x| < 1e6 A
+ *   bead_type, chain   nbead ints each, or NULL (all type 1, one chain);
+ *                      types must be 1 or 2
  *   nat_ptr, nat_idx   natives in CSR form (nat_ptr[nbead+1], partners of
  *                      bead i in nat_idx[nat_ptr[i]..nat_ptr[i+1]), sorted),
  *                      both listed per bead, or NULL for none
  *   pairs    2*cap ints: 1-based (i, j), i < j, in no particular order
- *   count    1 int: number of pairs found (only the first cap are written)
+ *   count    1 int: number of pairs found (only the first cap are written),
+ *            or, when the input is rejected and no pair is written, -1
+ *            (a position not finite or beyond 1e6 A) or -2 (a bead type
+ *            other than 1 or 2); read it after the stream has finished
  *   stream   a cudaStream_t, or NULL for the default stream
- * Result: the non-native neighbor list of neighbor_list.cpp:70-116 -- pairs
- * on different chains or |i-j| > 2 apart, not native, d^2 < (3.2 sigma)^2 in
- * FP64 -- as the set sop_update_neighbor_list + sop_get_pair_list(which=1)
- * give.  nbead > SOP_NOALLOC_MAX_BEADS returns SOP_ERR_UNSUPPORTED.  The
- * first call on a device looks up the scratch address there; make it before
- * any stream capture.  Calls share the scratch: calls that overlap on the GPU
+ * Result: the engine's non-native neighbor list of the system, the set
+ * sop_update_neighbor_list + sop_get_pair_list(which=1) give: pairs on
+ * different chains or |i-j| > 2 apart, not native, with d^2 < (3.2 sigma)^2
+ * in FP64, open boundaries (no minimum image; the engine flags a replica
+ * whose extent would need one with SOP_ST_PERIODIC).  nbead >
+ * SOP_NOALLOC_MAX_BEADS returns SOP_ERR_UNSUPPORTED.  The first call on a
+ * device looks up the scratch address there; make it before any stream
+ * capture.  Calls share the scratch: calls that overlap on the GPU
  * (different streams, or devices sharing it) race and must be ordered. */
 #define SOP_NOALLOC_MAX_BEADS 16384
 int sop_neighbor_list_noalloc(const double* xyz, int nbead, const int* bead_type, const int* chain,

@@ -4,15 +4,18 @@
 // device memory is owned by their own pool (a framework's caching allocator
 // that holds the GPU's memory), deployments that forbid allocation after
 // start-up, and latency-critical loops that cannot take the device-wide
-// synchronization a cudaMalloc or cudaFree may cause.  They pass device pointers for every input and
-// output; the binning scratch lives in one file-scope __device__ array of
-// fixed size (SOP_NOALLOC_MAX_BEADS beads), which every GPU that loads this
-// library holds until the process exits.
+// synchronization a cudaMalloc or cudaFree may cause.  They pass device
+// pointers for every input and output; the binning scratch lives in one
+// file-scope __device__ array of fixed size (SOP_NOALLOC_MAX_BEADS beads),
+// which every GPU that loads this library holds until the process exits.
 //
-// The list is the reference's non-native neighbor list (neighbor_list.cpp:
-// 70-116): pairs i<j that are on different chains or |i-j| > 2 apart, not
-// native, with d^2 < (3.2 sigma_ij)^2 decided in FP64 with the reference's
-// operation order.  Candidates come from a cell grid over the system.
+// The list is the engine's non-native neighbor list: pairs i<j on different
+// chains or |i-j| > 2 apart, not native, with d^2 < (3.2 sigma_ij)^2 decided
+// in FP64 in the same operation order as the engine's list build (open
+// boundaries: no minimum image).  Candidates come from a cell grid over the
+// system whose edge, and the FP32 pre-screen's margin, grow with the
+// system's extent, since relative FP32 positions carry an error of a few
+// units in the last place of the extent.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -29,8 +32,12 @@ constexpr int kBinThreads = 1024;
 
 struct GridInfo {
   float ox, oy, oz, edge;
+  float margin;  // relative margin of the FP32 pre-screen
   int nx, ny, nz, ok;
 };
+
+constexpr double kTwoM23 = 1.1920928955078125e-07;  // 2^-23
+constexpr double kRcMin = 3.2 * 3.8;                 // smallest list cutoff (type 1-1)
 
 // Scratch layout (bytes): P float4[kMaxBeads] | sorted int[kMaxBeads] |
 // cell int[kMaxBeads] | cstart int[kMaxCellsNA + 1] | ccur int[kMaxCellsNA] | GridInfo
@@ -70,23 +77,27 @@ __device__ __forceinline__ int type_of(const int* type, int i) { return type ? t
 __device__ __forceinline__ int chain_of(const int* chain, int i) { return chain ? chain[i] : 0; }
 
 // One CTA: bounding box, cell grid, stable counting sort of the beads into cells.
+// Rejected input (*count < 0, nothing else written): positions not finite or
+// beyond 1e6 A in magnitude (-1), a bead type other than 1 or 2 (-2).
 __global__ void __launch_bounds__(kBinThreads) k_na_bin(unsigned char* base, const double* xyz,
                                                        int n, const int* type, int* count) {
   Scratch S = scratch_at(base);
   __shared__ float red[6][kBinThreads / 32];
   __shared__ int s_tmask;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  if (tid == 0) { *count = 0; s_tmask = 0; }
+  if (tid == 0) s_tmask = 0;
   __syncthreads();
   float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
   int tm = 0;
   for (int i = tid; i < n; i += blockDim.x) {
     for (int c = 0; c < 3; c++) {
       const float v = (float)xyz[3 * (long long)i + c];
-      mn[c] = fminf(mn[c], v);
-      mx[c] = fmaxf(mx[c], v);
+      // a NaN never enters fminf/fmaxf: count it as out of range
+      mn[c] = v == v ? fminf(mn[c], v) : -3.4e38f;
+      mx[c] = v == v ? fmaxf(mx[c], v) : 3.4e38f;
     }
-    tm |= 1 << (type_of(type, i) & 3);
+    const int t = type_of(type, i);
+    tm |= (t == 1 || t == 2) ? (1 << t) : 1;  // bit 0: a bad type
   }
   for (int o = 16; o > 0; o >>= 1) {
     for (int c = 0; c < 3; c++) {
@@ -113,12 +124,26 @@ __global__ void __launch_bounds__(kBinThreads) k_na_bin(unsigned char* base, con
         if (((s_tmask >> a) & 1) && ((s_tmask >> b) & 1)) rmax = fmax(rmax, 3.2 * c_sigma[a][b]);
     GridInfo g;
     g.ok = 1;
-    for (int c = 0; c < 3; c++)
+    int reject = 0;
+    double ext = 0.0;
+    for (int c = 0; c < 3; c++) {
       if (!(isfinite(m0[c]) && isfinite(m1[c]) && m1[c] >= m0[c] && fabsf(m0[c]) < 1e6f &&
             fabsf(m1[c]) < 1e6f))
-        g.ok = 0;
-    // margin below 1 ulp of the origin shift keeps every in-range pair in adjacent cells
-    g.edge = (float)rmax * 1.0001f + 1e-3f;
+        reject = 1;
+      else
+        ext = fmax(ext, (double)m1[c] - (double)m0[c]);
+    }
+    if (!reject && (s_tmask & 1)) reject = 2;
+    if (reject) g.ok = 0;
+    // Relative positions P = float(x - origin) lie in [1, ext + 2) and carry
+    // up to half an ulp of that, 2^-24 (ext + 2); a cell index P / edge adds
+    // the same again.  perr bounds both with a factor two to spare.  Pairs
+    // within the cutoff then land in adjacent cells when the edge exceeds the
+    // cutoff by a few perr, and the FP32 pre-screen keeps every pair whose
+    // FP32 d^2 is within its own error of the cutoff.
+    const double perr = (ext + 2.0) * kTwoM23;
+    g.edge = (float)(rmax * 1.0001 + 6.0 * perr + 1e-3);
+    g.margin = (float)(1e-5 + 8.0 * perr / kRcMin);
     g.ox = m0[0] - 1.0f; g.oy = m0[1] - 1.0f; g.oz = m0[2] - 1.0f;
     for (;;) {
       g.nx = g.ok ? (int)((m1[0] - g.ox) / g.edge) + 1 : 1;
@@ -128,9 +153,11 @@ __global__ void __launch_bounds__(kBinThreads) k_na_bin(unsigned char* base, con
       g.edge *= 1.25f;
     }
     *S.grid = g;
+    *count = -reject;  // every call starts from zero pairs, or reports the rejection
   }
   __syncthreads();
   const GridInfo g = *S.grid;
+  if (!g.ok) return;
   const int ncell = g.nx * g.ny * g.nz;
   // every call reuses the scratch: counts start from zero
   for (int c = tid; c < ncell; c += blockDim.x) S.ccur[c] = 0;
@@ -213,9 +240,9 @@ __global__ void k_na_enum(unsigned char* base, const double* xyz, int n, const i
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float d2f = dx * dx + dy * dy + dz * dz;
         const int tj = type_of(type, j);
-        const double rc = 3.2 * c_sigma[ti][tj];  // neighbor_list.cpp:97-100
+        const double rc = 3.2 * c_sigma[ti][tj];
         const double rc2 = rc * rc;
-        if (d2f > (float)rc2 * 1.0001f) continue;
+        if (d2f > (float)rc2 * (1.0f + g.margin)) continue;
         // the decision itself in FP64 with the reference's order, no FMA
         const double ex = __dsub_rn(xyz[3 * (long long)j], xyz[3 * (long long)i]);
         const double ey = __dsub_rn(xyz[3 * (long long)j + 1], xyz[3 * (long long)i + 1]);
