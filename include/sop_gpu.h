@@ -82,7 +82,9 @@ typedef struct sop_params {
   double k_bnd, R0;          /* FENE (params.cpp:268-271)                    */
   double sigma_ss, epsilon_ss; /* i,i+2 soft sphere (params.cpp:289-293)     */
   double skin;    /* SOP_LIST_SKIN: list cutoff is 2.5 sigma + skin, A       */
-  double cell_edge; /* spatial-grid edge used by the list build, A (0=auto)  */
+  double cell_edge; /* edge of the list build's cell grid, A: at least half
+                       the list cutoff (smaller values and 0 give that half;
+                       5x5x5 stencil), from the cutoff up a 3x3x3 stencil   */
   double pull_force; /* constant force on the two termini along their
                         separation, kcal/mol/A (0 = off; no reference term)  */
   uint64_t seed;  /* counter-based noise key                                */
@@ -120,7 +122,9 @@ typedef struct sop_engine_config {
   int max_beads;         /* bead capacity of the packed arrays (0 = 1<<21)     */
   int max_replicas;      /* replica slots (0 = 4096)                           */
   int64_t max_list_entries; /* neighbor-list entry capacity (0 = 64 per bead)  */
-  int block_threads;     /* fused step kernel block size, 64..256 (0 = 256)   */
+  int block_threads;     /* fused step kernel block size, 64..512, multiple of
+                            32 (0 = 256); 512 with lanes_per_bead 1, 2 or 4
+                            and step_strategy 0 only (else UNSUPPORTED)     */
   int lanes_per_bead;    /* lanes cooperating on one bead: 1,2,4,8,16 (0 = 2)  */
   int graph_steps;       /* steps captured per CUDA graph launch (0 = 20)      */
   int stage_limit;       /* largest replica (beads) whose positions the step
@@ -279,9 +283,10 @@ int sop_replica_restore(sop_engine* e, int replica, const void* buf, int64_t siz
 /* ---- autotuner --------------------------------------------------------------- */
 /* No reference counterpart.  Time the batched step of the active replicas
  * over candidate launch shapes (step strategy, stage limit, beads per work
- * item, block size, lanes per bead, register budget, beads per list-build
- * slice, rebuild grouping; one choice for the engine) and, for replicas in
- * skin mode, list skins and cell edges (one choice per size bucket
+ * item, block size 64-512, lanes per bead, register budget, beads per
+ * list-build slice, rebuild grouping; one choice for the engine) and, for
+ * replicas in skin mode, list skins 1-4 A and cell edges 6-12 A (one choice
+ * per size bucket
  * [1,256) [256,1024) [1024,4096) [4096,...)); adopt the fastest.
  * Every trial runs steps_per_trial warm-up plus steps_per_trial timed REAL
  * steps inside one run window, so the call advances each active replica

@@ -1,7 +1,7 @@
 // Autotuner of the batched step: launch shape (step strategy, stage limit,
-// beads per work item, block size, lanes per bead, register budget, build
-// slice, rebuild grouping) for the whole engine, and list parameters (skin,
-// cell edge) per replica size bucket.
+// beads per work item, block size 64-512, lanes per bead, register budget,
+// build slice, rebuild grouping) for the whole engine, and list parameters
+// (skin 1-4 A, cell edge 6-12 A) per replica size bucket.
 //
 // Every trial is a run of real steps: the tuner opens one run window over all
 // its trials for every active replica, so sop_autotune advances the replicas
@@ -127,14 +127,16 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
       {"warp", &LaunchShape::strategy, {0, 1}},
       {"stage", &LaunchShape::stage, stages},
       {"chunk", &LaunchShape::chunk, {64, 128, 256, 512}},
-      {"threads", &LaunchShape::threads, {64, 128, 256}},
+      {"threads", &LaunchShape::threads, {64, 128, 256, 512}},
       {"lanes", &LaunchShape::lanes, {1, 2, 4}},
       {"occ", &LaunchShape::min_blocks, {2, 3, 4}},
       {"slice", &LaunchShape::slice, {16, 32, 64, 128}},
       {"group", &LaunchShape::group_pct, {0, 30, 50, 70}},
   };
   const std::vector<double> skins = {1.0, 1.5, 2.0, 3.0, 4.0};
-  const std::vector<double> edge_pads = {0.0, 2.0, 4.0};
+  // absolute cell edges (A); the build widens an edge below half the list
+  // cutoff to that half, and 0 is that half exactly
+  const std::vector<double> edges = {0.0, 6.0, 7.0, 8.0, 9.0, 10.0, 11.0, 12.0};
   std::vector<Bucket> buckets = {{1, 256, {}}, {256, 1024, {}}, {1024, 4096, {}}, {4096, 1 << 30, {}}};
   if (what & SOP_TUNE_LISTS) {
     for (int r : e->active) {
@@ -151,7 +153,7 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
   int ntrials = 1;
   if (what & SOP_TUNE_SHAPE)
     for (const Knob& k : knobs) ntrials += (int)k.values.size();
-  for (size_t b = 0; b < buckets.size(); b++) ntrials += (int)(skins.size() + edge_pads.size());
+  for (size_t b = 0; b < buckets.size(); b++) ntrials += (int)(skins.size() + edges.size());
   Tuner T{e, steps_per_trial, (int64_t)ntrials * 2 * steps_per_trial, std::string()};
   const int64_t total = T.left;
   rc = begin_all(e, total);
@@ -176,6 +178,7 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
       for (int v : k.values) {
         LaunchShape s = cur;
         s.*(k.field) = v;
+        if (!step_shape_supported(s.lanes, s.strategy, s.threads)) continue;
         set_launch_shape(e, s);
         double ms = 0;
         if ((rc = T.trial(&ms))) return rc;
@@ -186,8 +189,6 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
       }
   }
 
-  const FFTables& F = tables();
-  const double rc_pl = 2.5 * std::max(F.sigma_rep[1][1], F.sigma_rep[2][2]);
   for (auto& b : buckets) {
     const Replica& R0 = e->reps[b.ids[0]];
     double best_skin = R0.params.skin, best_edge = R0.params.cell_edge, bms = 1e300;
@@ -206,8 +207,7 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
              b.ids.size(), s, best_edge, ms);
       if (ms < bms * 0.99) { bms = ms; best_skin = s; }
     }
-    for (double pad : edge_pads) {
-      const double edge = pad > 0 ? rc_pl + best_skin + pad : 0.0;
+    for (double edge : edges) {
       rc = set_lists(e, b.ids, best_skin, edge);
       if (rc) return rc;
       double ms = 0;

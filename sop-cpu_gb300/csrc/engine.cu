@@ -364,7 +364,9 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
   if (cfg.device < 0 || cfg.device >= ndev) return SOP_ERR_ARG;
   int lanes = cfg.lanes_per_bead;
   if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16) return SOP_ERR_ARG;
-  if (cfg.block_threads % 32 || cfg.block_threads < 64 || cfg.block_threads > 256) return SOP_ERR_ARG;
+  if (cfg.block_threads % 32 || cfg.block_threads < 64 || cfg.block_threads > 512) return SOP_ERR_ARG;
+  if (!step_shape_supported(cfg.lanes_per_bead, cfg.step_strategy, cfg.block_threads))
+    return SOP_ERR_UNSUPPORTED;
   std::unique_ptr<sop_engine> e(new (std::nothrow) sop_engine());
   if (!e) return SOP_ERR_NOMEM;
   e->cfg = cfg;

@@ -263,10 +263,12 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
         h.K = 1;
         if ((long long)h.nx * h.ny * h.nz > ccap) h.status |= SOP_ST_GRID;
       } else if (mode != SOP_LIST_NONE) {
-        // cells half a list cutoff wide: a 5x5x5 stencil reaches one cutoff
-        float full = fmaxf(R->cell_edge, rl_max * 1.0001f + 1e-3f);
+        // cells of the replica's cell edge, at least half a list cutoff wide
+        // (0 = exactly half): K cells each way reach one cutoff, a 5x5x5
+        // stencil below the cutoff, 3x3x3 from the cutoff up
+        const float rcut = rl_max * 1.0001f + 1e-3f;
+        float e = fmaxf(R->cell_edge, 0.5f * rcut);
         for (;;) {
-          const float e = 0.5f * full;
           const long long nx = (long long)((m1[0] - m0[0]) / e) + 1;
           const long long ny = (long long)((m1[1] - m0[1]) / e) + 1;
           const long long nz = (long long)((m1[2] - m0[2]) / e) + 1;
@@ -275,9 +277,9 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
             h.edge = e;
             break;
           }
-          full *= 1.25f;
+          e *= 1.25f;
         }
-        h.K = 2;
+        h.K = e >= rcut ? 1 : 2;
       }
       h.ncell = h.nx * h.ny * h.nz;
       h.ok = !(h.status & SOP_ST_GRID);
@@ -1255,9 +1257,10 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   bead_tail<ST>(A, C, S, b, Fx, Fy, Fz, st);
 }
 
-// MB: resident CTAs per SM the register allocation is sized for (2 or 3)
-template <int G, int MB>
-__global__ void __launch_bounds__(256, MB) k_step(DevArrays A, const StepItem* items,
+// TPB: largest block size (256, or 512 for the wide variants); MB: resident
+// CTAs of TPB threads per SM the register allocation is sized for
+template <int G, int MB, int TPB = 256>
+__global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* items,
                                                  const int* nitems_dev, int nitems_host) {
   const int nitems = nitems_dev ? *nitems_dev : nitems_host;
   extern __shared__ __align__(128) float4 sst[];
@@ -1862,7 +1865,26 @@ static StepKernel step_kernel_g(int strategy, int min_blocks) {
   if (min_blocks == 4) return k_step<G, 4>;
   return two ? k_step<G, 2> : k_step<G, 3>;
 }
-static StepKernel step_kernel(int lanes, int min_blocks, int strategy) {
+// 512-thread CTAs: the register budget of min_blocks 256-thread CTAs per SM
+// (4 -> two 512-thread CTAs at 64 registers, 2 or 3 -> one at up to 128)
+template <int G>
+static StepKernel step_kernel_wide(int min_blocks) {
+  return min_blocks == 4 ? k_step<G, 2, 512> : k_step<G, 1, 512>;
+}
+bool step_shape_supported(int lanes, int strategy, int threads) {
+  if (threads % 32 || threads < 64 || threads > 512) return false;
+  if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16) return false;
+  if (threads > 256) return strategy == 0 && lanes <= 4;
+  return true;
+}
+static StepKernel step_kernel(int lanes, int min_blocks, int strategy, int threads = 256) {
+  if (threads > 256) {
+    switch (lanes) {
+      case 1: return step_kernel_wide<1>(min_blocks);
+      case 2: return step_kernel_wide<2>(min_blocks);
+      default: return step_kernel_wide<4>(min_blocks);
+    }
+  }
   switch (lanes) {
     case 1: return step_kernel_g<1>(strategy, min_blocks);
     case 2: return step_kernel_g<2>(strategy, min_blocks);
@@ -1892,8 +1914,11 @@ cudaError_t init_kernels(int optin_bytes, int sm_bytes) {
   const int half = std::min(optin_bytes, sm_bytes / 2);
   if ((e = optin(k_prep, half, &g_prep_dyn)) != cudaSuccess) return e;
   for (int lanes : {1, 2, 4, 8, 16})
-    for (int mb : {2, 3, 4})
+    for (int mb : {2, 3, 4}) {
       if ((e = optin(step_kernel(lanes, mb, 0), optin_bytes)) != cudaSuccess) return e;
+      if (lanes <= 4 && (e = optin(step_kernel(lanes, mb, 0, 512), optin_bytes)) != cudaSuccess)
+        return e;
+    }
   return cudaSuccess;
 }
 
@@ -1928,7 +1953,9 @@ cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, c
   if (nitems <= 0) return cudaSuccess;
   const size_t dyn = strategy == 1 ? 0 : (size_t)max_staged * 32 + 128;
   if (grid <= 0) grid = nitems;
-  step_kernel(lanes, min_blocks, strategy)<<<grid, threads, dyn, s>>>(A, items, nitems_dev, nitems);
+  if (!step_shape_supported(lanes, strategy, threads)) return cudaErrorInvalidConfiguration;
+  step_kernel(lanes, min_blocks, strategy, threads)<<<grid, threads, dyn, s>>>(A, items, nitems_dev,
+                                                                              nitems);
   return cudaGetLastError();
 }
 
@@ -1937,7 +1964,8 @@ int step_kernel_max_smem() { return kStageMax * 32 + 128; }
 int step_blocks_per_sm(int lanes, int min_blocks, int strategy, int threads, int max_staged) {
   const size_t dyn = strategy == 1 ? 0 : (size_t)max_staged * 32 + 128;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel(lanes, min_blocks, strategy),
+  if (!step_shape_supported(lanes, strategy, threads)) return 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel(lanes, min_blocks, strategy, threads),
                                                     threads, dyn) != cudaSuccess) {
     cudaGetLastError();
     return 1;

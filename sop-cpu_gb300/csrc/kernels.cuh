@@ -135,5 +135,8 @@ cudaError_t launch_export(const DevArrays& A, int r, int off, int n, int which, 
 int step_kernel_max_smem();
 // resident step-kernel CTAs per SM for this configuration
 int step_blocks_per_sm(int lanes, int min_blocks, int strategy, int threads, int max_staged);
+// block sizes 64..256 (multiples of 32) for every lanes / strategy; 512 for
+// the CTA strategy with 1, 2 or 4 lanes per bead
+bool step_shape_supported(int lanes, int strategy, int threads);
 
 }  // namespace sop

@@ -82,7 +82,10 @@ def test_list_tuning_keeps_reference_pair_sets():
                                  dict(step_min_blocks=3, stage_limit=2048), dict(step_min_blocks=2),
                                  dict(stage_limit=-1), dict(build_slice_beads=128, chunk_beads=64),
                                  dict(lanes_per_bead=4), dict(lanes_per_bead=1),
-                                 dict(group_rebuild_pct=-1), dict(group_rebuild_pct=90)])
+                                 dict(group_rebuild_pct=-1), dict(group_rebuild_pct=90),
+                                 dict(block_threads=512), dict(block_threads=512, step_min_blocks=3,
+                                                               chunk_beads=256),
+                                 dict(block_threads=512, lanes_per_bead=4, stage_limit=-1)])
 def test_launch_shapes_bit_identical(cfg):
     """Every launch shape, both step strategies (CTA items staged in shared
     memory, warp tasks through L1/L2), every lane count and rebuild grouping
@@ -99,3 +102,30 @@ def test_launch_shapes_bit_identical(cfg):
             out.append([e.state(r)[1] for r in ids])
     for a, b in zip(*out):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("edge", [6.0, 8.0, 10.0, 12.0, 16.0])
+def test_cell_edges_keep_pair_sets_and_trajectories(edge):
+    """Absolute cell edges of the list build's grid (list cutoff 2.5 sigma +
+    2 A = 11.5 A: 6-10 A cells with the 5x5x5 stencil, 12 and 16 A with the
+    3x3x3 one): the same pair sets and trajectory as the reference cadence."""
+    systems = [S.synth_chain(8500 + k, n) for k, n in enumerate([90, 700, 2600])]
+    with engine() as e:
+        ref = [e.add(s, make_params(script(), force_terms=DET)) for s in systems]
+        skin = [e.add(s, make_params(script(), force_terms=DET, list_mode="skin", skin=2.0,
+                                     cell_edge=edge)) for s in systems]
+        for _ in range(2):
+            e.run(200)
+            for a, b in zip(ref, skin):
+                for k in (2, 3):
+                    np.testing.assert_array_equal(pairset(*e.pairs(a, k)), pairset(*e.pairs(b, k)))
+                np.testing.assert_array_equal(e.state(a)[1], e.state(b)[1])
+                assert e.status(b)[0] == 0
+
+
+def test_block_size_outside_the_supported_shapes_is_refused():
+    with pytest.raises(Exception):
+        Engine(0, max_beads=1 << 12, max_replicas=4, max_list_entries=1 << 20, block_threads=512,
+               step_strategy=1)
+    with pytest.raises(Exception):
+        Engine(0, max_beads=1 << 12, max_replicas=4, max_list_entries=1 << 20, block_threads=576)
