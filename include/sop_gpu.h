@@ -40,6 +40,8 @@ extern "C" {
 #define SOP_ERR_NODEV -7       /* no usable CUDA device                         */
 #define SOP_ERR_REPLICA -8     /* a replica carries an error status (see below) */
 #define SOP_ERR_FULL -9        /* no room: admission refused, retry later        */
+#define SOP_ERR_TIMEOUT -10    /* a bounded device-side wait ran out; the replicas
+                                  stepped in that call are in an undefined state */
 
 /* per-replica status bits (sop_replica_status) */
 #define SOP_ST_NONFINITE 0x1     /* NaN/inf force or position                   */
@@ -147,6 +149,15 @@ typedef struct sop_engine_config {
                             phase when the previous step flagged no possible
                             work (no skin trigger, output, observables or
                             cadence build): 0 = on, <0 = off (same results)   */
+  /* Limits of the two device-side waits (0 = 2 s each; at most 60 s).  Neither
+   * is expected to run out: a CTA of the preparation kernel waits for a work
+   * unit another CTA is still publishing, and a step-kernel CTA waits for
+   * its bulk copy of positions into shared memory.  A wait that runs out
+   * records it, lets its copies in flight land, and returns; the call then
+   * fails with SOP_ERR_TIMEOUT and the engine clears the queue, so later
+   * calls work (restore or re-add the replicas that call stepped). */
+  int64_t queue_wait_ns;
+  int64_t stage_wait_ns;
 } sop_engine_config;
 
 /* ---- engine -------------------------------------------------------------- */
@@ -165,6 +176,17 @@ int sop_engine_launches(const sop_engine* e, int64_t* launches);
 /* preparation launches that skipped the work-queue phase but found queued work
  * all the same and ran it in one CTA (correct, slower; expected to stay 0) */
 int sop_engine_prep_fallbacks(sop_engine* e, int64_t* count);
+/* Diagnostics, no reference counterpart: host-controlled stalls that make the
+ * device-side waits above run out, for tests of the timeout path (no fault,
+ * no unbounded wait).  publish_delay_ns (0..1e9): every preparation CTA that
+ * publishes list-build units first waits that long; skip_stage_copy != 0: the
+ * step kernel's CTAs expect their position copies but do not issue them.
+ * Both 0 = normal operation.  Call between runs. */
+int sop_engine_inject_stall(sop_engine* e, int64_t publish_delay_ns, int skip_stage_copy);
+/* Which waits ran out in the call that last returned SOP_ERR_TIMEOUT:
+ * bit 0 the step kernel's copy wait, bit 1 the preparation kernel's queue
+ * wait (0 if none since the engine was created). */
+int sop_engine_wait_errors(sop_engine* e, int* bits);
 
 /* ---- replicas ------------------------------------------------------------- */
 /* Upload a system; builds its lists at the initial positions (the set-up of

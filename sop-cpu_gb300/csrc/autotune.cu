@@ -51,6 +51,7 @@ struct Tuner {
 
   // S warm-up steps, then S timed steps: milliseconds per step
   int trial(double* ms_per_step) {
+    NvtxRange range("autotune trial");
     float ms = 0;
     int rc = run_steps(e, S, nullptr);
     if (rc) return rc;

@@ -137,6 +137,7 @@ extern "C" const char* sop_status_string(int s) {
     case SOP_ERR_NODEV: return "no CUDA device";
     case SOP_ERR_REPLICA: return "replica error status";
     case SOP_ERR_FULL: return "engine full";
+    case SOP_ERR_TIMEOUT: return "a bounded device-side wait ran out";
     default: return "unknown";
   }
 }
@@ -195,6 +196,8 @@ extern "C" void sop_engine_config_default(sop_engine_config* c) {
   c->build_slice_beads = kSliceBeads;
   c->step_min_blocks = 4;
   c->group_rebuild_pct = 50;
+  c->queue_wait_ns = kDefaultWaitNs;
+  c->stage_wait_ns = kDefaultWaitNs;
 }
 
 // ---- engine lifetime ------------------------------------------------------------
@@ -255,6 +258,10 @@ static int engine_init(sop_engine* e) {
                       ? (float)(0.01 * cfg.group_rebuild_pct * 0.01 * cfg.group_rebuild_pct)
                       : 4.0f;
   CK(cudaMemsetAsync(A.err, 0, sizeof(int), e->stream));
+  A.queue_wait_ns = cfg.queue_wait_ns;
+  A.stage_wait_ns = cfg.stage_wait_ns;
+  A.publish_delay_ns = 0;
+  A.skip_stage_copy = 0;
   // unit queue: every replica may queue all its build slices plus two units
   A.slice_beads = cfg.build_slice_beads;
   // every replica may queue all its build slices (at the smallest slice size)
@@ -348,6 +355,8 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
     if (cfg_in->step_strategy > 0) cfg.step_strategy = cfg_in->step_strategy;
     if (cfg_in->group_rebuild_pct != 0) cfg.group_rebuild_pct = cfg_in->group_rebuild_pct;
     cfg.lean_prep = cfg_in->lean_prep < 0 ? -1 : 0;
+    if (cfg_in->queue_wait_ns > 0) cfg.queue_wait_ns = std::min<int64_t>(cfg_in->queue_wait_ns, kMaxWaitNs);
+    if (cfg_in->stage_wait_ns > 0) cfg.stage_wait_ns = std::min<int64_t>(cfg_in->stage_wait_ns, kMaxWaitNs);
   }
   if (cfg.group_rebuild_pct < 0 || cfg.group_rebuild_pct >= 100) cfg.group_rebuild_pct = 0;
   if (cfg.step_strategy != 1) cfg.step_strategy = 0;
@@ -1011,6 +1020,7 @@ extern "C" int sop_system_bytes(const sop_engine* e, const sop_system_desc* d, i
 
 extern "C" int sop_replicas_admit(sop_engine* e, sop_prepared* const* p, const int64_t* nsteps, int n,
                                   int* ids, int* admitted) {
+  NvtxRange range("admit replicas");
   if (!e || (n > 0 && (!p || !ids)) || !admitted || n < 0) return SOP_ERR_ARG;
   *admitted = 0;
   if (n == 0) return SOP_OK;
@@ -1062,6 +1072,7 @@ extern "C" int sop_replicas_admit(sop_engine* e, sop_prepared* const* p, const i
 }
 
 extern "C" int sop_replica_add(sop_engine* e, const sop_system_desc* d, int* replica) {
+  NvtxRange range("add replica");
   if (!e || !replica) return SOP_ERR_ARG;
   sop_prepared P;
   int rc = prepare(d, P);
@@ -1324,6 +1335,7 @@ int sop::refresh_layout(sop_engine* e) {
 // One step over given ids / items with host counts (single-replica paths).
 int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items,
                       int nitems, int max_staged, int step_grid, int pro_grid, bool fp64) {
+  NvtxRange range("plain step: k_prep + k_step");
   CK(launch_prologue(e->A, d_ids, nrep, nullptr, 0, 0, 1, pro_grid, e->stream));
   if (fp64)
     CK(launch_step64(e->A, d_items, nitems, nullptr, step_grid, e->stream));
@@ -1340,6 +1352,7 @@ int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem*
 // full: the first step after host-side work (every later k_prep reads the
 // device-side work flags the previous one left).
 int sop::enqueue_batched_step(sop_engine* e, bool full) {
+  NvtxRange range("batched step: k_prep + k_step");
   CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0,
                      (full || e->cfg.lean_prep < 0) ? 1 : 0,
                      e->pro_grid, e->stream));
@@ -1372,16 +1385,47 @@ __global__ void k_set_phase(RepDev* rep, int r, int phase) {
   R->out = 0;
 }
 
+// A bounded device wait ran out (error word `err`, already read back):
+// remember which, clear the word and the work queue (a unit published after
+// its consumer gave up would otherwise be taken by the next step), and report.
+static int timed_out(sop_engine* e, int err) {
+  e->wait_errors = err;
+  CK(cudaMemsetAsync(e->A.err, 0, sizeof(int), e->stream));
+  CK(cudaMemsetAsync(e->A.units, 0xFF, sizeof(int4) * e->A.unit_cap, e->stream));
+  CK(cudaMemsetAsync(e->A.unit_cnt, 0, sizeof(int), e->stream));
+  CK(cudaMemsetAsync(e->A.unit_take, 0, sizeof(int), e->stream));
+  CK(cudaMemsetAsync(e->A.unit_exit, 0, sizeof(int), e->stream));
+  CK(cudaMemsetAsync(e->A.pro_done, 0, sizeof(int), e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  e->graph_valid = false;
+  return SOP_ERR_TIMEOUT;
+}
+
 static int check_errors(sop_engine* e) {
   int err = 0;
   CK(cudaMemcpyAsync(&err, e->A.err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
   CK(cudaStreamSynchronize(e->stream));
-  return err ? SOP_ERR_CUDA : SOP_OK;
+  return err ? timed_out(e, err) : SOP_OK;
+}
+
+extern "C" int sop_engine_inject_stall(sop_engine* e, int64_t publish_delay_ns, int skip_stage_copy) {
+  if (!e || publish_delay_ns < 0 || publish_delay_ns > 1000000000LL) return SOP_ERR_ARG;
+  e->A.publish_delay_ns = publish_delay_ns;
+  e->A.skip_stage_copy = skip_stage_copy ? 1 : 0;
+  e->graph_valid = false;  // kernels take the device arrays by value
+  return SOP_OK;
+}
+
+extern "C" int sop_engine_wait_errors(sop_engine* e, int* bits) {
+  if (!e || !bits) return SOP_ERR_ARG;
+  *bits = e->wait_errors;
+  return SOP_OK;
 }
 
 // ---- plain single-system path ------------------------------------------------------
 
 extern "C" int sop_run_plain(sop_engine* e, int r, int64_t nsteps) {
+  NvtxRange range("sop_run_plain");
   if (!e || !live(e, r) || nsteps < 0) return SOP_ERR_ARG;
   if (nsteps == 0) return SOP_OK;
   Replica& R = e->reps[r];
@@ -1421,6 +1465,7 @@ extern "C" int sop_run_plain(sop_engine* e, int r, int64_t nsteps) {
 
 static int capture_graph(sop_engine* e) {
   if (e->graph_valid) return SOP_OK;
+  NvtxRange range("capture step graph");
   if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
@@ -1452,9 +1497,12 @@ int sop::run_batched(sop_engine* e, int64_t nsteps, bool timed) {
   const int64_t iters = nsteps + 1;
   const int S = e->cfg.graph_steps;
   const int64_t full = iters / S;
-  for (int64_t k = 0; k < full; k++) {
-    CK(cudaGraphLaunch(e->graph_exec, e->stream));
-    e->launches += e->graph_launches;
+  {
+    NvtxRange graphs("graph launches");
+    for (int64_t k = 0; k < full; k++) {
+      CK(cudaGraphLaunch(e->graph_exec, e->stream));
+      e->launches += e->graph_launches;
+    }
   }
   for (int64_t k = full * S; k < iters; k++) {
     rc = enqueue_batched_step(e, k == full * S);
@@ -1486,6 +1534,7 @@ extern "C" int sop_replica_start(sop_engine* e, int r, int64_t nsteps) {
 
 extern "C" int sop_replicas_retire(sop_engine* e, const int* ids, int n, double* energy6, double* obs5,
                                    int* status) {
+  NvtxRange range("retire replicas");
   if (!e || n < 0 || (n > 0 && !ids) || n > e->cfg.max_replicas) return SOP_ERR_ARG;
   if (n == 0) return SOP_OK;
   std::vector<char> seen(e->cfg.max_replicas, 0);
@@ -1527,6 +1576,7 @@ extern "C" int sop_replicas_retire(sop_engine* e, const int* ids, int n, double*
 }
 
 extern "C" int sop_run_chunk_begin(sop_engine* e, int64_t steps) {
+  NvtxRange range("run chunk: launch");
   if (!e || steps < 0) return SOP_ERR_ARG;
   if (e->chunk_open) return SOP_ERR_STATE;
   CK(cudaSetDevice(e->cfg.device));
@@ -1553,6 +1603,7 @@ extern "C" int sop_run_chunk_begin(sop_engine* e, int64_t steps) {
 }
 
 extern "C" int sop_run_chunk_end(sop_engine* e, int* finished, int cap, int* nfinished) {
+  NvtxRange range("run chunk: wait");
   if (!e || (cap > 0 && !finished)) return SOP_ERR_ARG;
   if (nfinished) *nfinished = 0;
   if (!e->chunk_open) return SOP_OK;
@@ -1646,6 +1697,7 @@ void sop::set_launch_shape(sop_engine* e, const LaunchShape& s) {
 
 extern "C" int sop_run(sop_engine* e, int64_t nsteps) {
   if (!e || nsteps < 0) return SOP_ERR_ARG;
+  NvtxRange range("sop_run");
   CK(cudaSetDevice(e->cfg.device));
   return run_batched(e, nsteps, true);
 }
@@ -1812,6 +1864,7 @@ static int run_phase(sop_engine* e, int r, int phase) {
 }
 
 extern "C" int sop_force_eval(sop_engine* e, int r, double* force_xyz) {
+  NvtxRange range("sop_force_eval");
   if (!e || !live(e, r)) return SOP_ERR_ARG;
   int rc = run_phase(e, r, PH_FORCE);
   if (rc) return rc;
@@ -1830,6 +1883,7 @@ extern "C" int sop_force_eval(sop_engine* e, int r, double* force_xyz) {
 }
 
 extern "C" int sop_energy_eval(sop_engine* e, int r, double* out) {
+  NvtxRange range("sop_energy_eval");
   if (!e || !live(e, r)) return SOP_ERR_ARG;
   CK(cudaMemcpyAsync(e->d_ids + scratch_id(e, 0), &r, sizeof(int), cudaMemcpyHostToDevice, e->stream));
   int rc_e = enqueue_energy(e, &r, e->d_ids + scratch_id(e, 0), 1);

@@ -1,6 +1,7 @@
 // Internal host-side state of the GB300 SOP engine (not part of the C ABI).
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -50,6 +51,18 @@ const FFTables& tables();
 
 }  // namespace sop
 
+// Named host-side ranges for profilers (NVTX v3, header-only: without an
+// attached tool each push / pop is a cheap no-op).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
+constexpr int64_t kDefaultWaitNs = 2000000000LL;  // device-side wait limits: 2 s
+constexpr int64_t kMaxWaitNs = 60000000000LL;
+
 struct sop_engine {
   sop_engine_config cfg{};
   cudaDeviceProp prop{};
@@ -90,6 +103,7 @@ struct sop_engine {
   int pairs_cap = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int64_t launches = 0;
+  int wait_errors = 0;  // error-word bits of the last call that timed out
   int64_t graph_launches = 0;  // launches of one replay of the step graph
   double last_total_ms = 0, last_step_ms = -1;
   int64_t last_step_launches = 0;

@@ -798,7 +798,9 @@ __device__ void run_unit(const DevArrays& A, int4 w, BuildSmem& B, unsigned char
   }
 }
 
-constexpr unsigned long long kQueueWaitNs = 2000000000ULL;  // 2 s: never expected
+// After a staging wait ran out: how long the CTA lets its copy in flight land
+// before it leaves (a copy of at most 227 KB takes microseconds).
+constexpr unsigned long long kDrainNs = 10000000ULL;  // 10 ms
 
 // K0 + K1 + K2 of a step in one cooperative launch (every CTA resident).
 // Producers: CTA b owns the replicas k = b, b + grid, ...; its threads do
@@ -846,6 +848,13 @@ __global__ void __launch_bounds__(kBuildThreads, 2) k_prep(DevArrays A, const in
       // the bins (written by the whole CTA) before the slices that read them
       __threadfence();
       __syncthreads();
+      if (A.publish_delay_ns > 0) {  // diagnostics: a host-requested stall (bounded)
+        if (threadIdx.x == 0) {
+          const unsigned long long t0 = globaltimer_ns();
+          while (globaltimer_ns() - t0 < (unsigned long long)A.publish_delay_ns) __nanosleep(1000);
+        }
+        __syncthreads();
+      }
       const int nsl = (A.rep[r].n + sb - 1) / sb;
       if (threadIdx.x == 0) s_base = atomicAdd(A.unit_cnt, nsl);
       __syncthreads();
@@ -887,8 +896,8 @@ __global__ void __launch_bounds__(kBuildThreads, 2) k_prep(DevArrays A, const in
             if (t >= min(ld_volatile(A.unit_cnt), A.unit_cap)) break;  // drained
             continue;
           }
-          if (globaltimer_ns() - t0 > kQueueWaitNs) {  // never expected: record and stop
-            atomicOr(A.err, 2);
+          if (globaltimer_ns() - t0 > (unsigned long long)A.queue_wait_ns) {
+            atomicOr(A.err, 2);  // never expected: record and stop waiting
             break;
           }
         }
@@ -1297,22 +1306,33 @@ __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* i
         const uint32_t bytes = (uint32_t)C.n * 32u;
         fence_async_smem();
         mbar_expect_tx(&mbar, bytes);
-        for (uint32_t o = 0; o < bytes; o += 32768u) {
-          const uint32_t b = (bytes - o < 32768u) ? bytes - o : 32768u;
-          tma_bulk_g2s(reinterpret_cast<char*>(sst) + o, src + o, b, &mbar);
-        }
+        if (!A.skip_stage_copy)  // (diagnostics: expected but not issued)
+          for (uint32_t o = 0; o < bytes; o += 32768u) {
+            const uint32_t b = (bytes - o < 32768u) ? bytes - o : 32768u;
+            tma_bulk_g2s(reinterpret_cast<char*>(sst) + o, src + o, b, &mbar);
+          }
       }
     }
     __syncthreads();
     const ItemCtx C = sC;
     if (C.phase != PH_SKIP) {
       if (w.staged) {
-        long long spins = 0;
+        const unsigned long long t0 = globaltimer_ns();
+        bool late = false;
         while (!mbar_try_wait(&mbar, parity)) {
-          if (++spins > (1LL << 26)) {  // never expected: record and stop waiting
-            atomicOr(A.err, 1);
+          if (globaltimer_ns() - t0 > (unsigned long long)A.stage_wait_ns) {
+            late = true;
             break;
           }
+        }
+        if (__syncthreads_or(late)) {
+          // never expected: record it, let the copy in flight land in this
+          // CTA's shared memory (bounded), and leave the step
+          if (threadIdx.x == 0) atomicOr(A.err, 1);
+          const unsigned long long t1 = globaltimer_ns();
+          while (!mbar_try_wait(&mbar, parity) && globaltimer_ns() - t1 < kDrainNs) {
+          }
+          return;
         }
         parity ^= 1u;
         for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, true>(A, C, sst, b, lane, gmask);

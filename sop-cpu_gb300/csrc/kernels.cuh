@@ -31,6 +31,10 @@ struct DevArrays {
   unsigned long long* pairs_out;  // export buffer (i<<32|j)
   int* pairs_cnt;
   int* err;           // engine-wide error word (bounded waits that gave up)
+  long long queue_wait_ns;     // k_prep: wait for a unit being published
+  long long stage_wait_ns;     // k_step: wait for the staging copy
+  long long publish_delay_ns;  // diagnostics: producers stall before publishing
+  int skip_stage_copy;         // diagnostics: staging copies expected, not issued
   int4* units;        // per-step work queue (builds in slices, energies, observables)
   int* unit_cnt;      // units queued this step
   int* unit_exit;     // k_prep CTAs finished (the last one resets the queue)

@@ -18,8 +18,9 @@ SOP_OK = 0
 ERRORS = {
     -1: "SOP_ERR_ARG", -2: "SOP_ERR_CUDA", -3: "SOP_ERR_NOMEM", -4: "SOP_ERR_STATE",
     -5: "SOP_ERR_OVERFLOW", -6: "SOP_ERR_UNSUPPORTED", -7: "SOP_ERR_NODEV",
-    -8: "SOP_ERR_REPLICA", -9: "SOP_ERR_FULL",
+    -8: "SOP_ERR_REPLICA", -9: "SOP_ERR_FULL", -10: "SOP_ERR_TIMEOUT",
 }
+ERR_TIMEOUT = -10
 ST_NONFINITE, ST_FENE, ST_LIST_OVERFLOW, ST_PERIODIC, ST_GRID = 1, 2, 4, 8, 16
 LIST_NONE, LIST_NEIGHBOR, LIST_CELL, LIST_SKIN = 0, 1, 2, 3
 TERM_RANDOM, TERM_FENE, TERM_ANGLE, TERM_VDW, TERM_ALL = 1, 2, 4, 8, 15
@@ -77,7 +78,7 @@ class EngineConfig(C.Structure):
         ("lanes_per_bead", C.c_int), ("graph_steps", C.c_int),
         ("stage_limit", C.c_int), ("chunk_beads", C.c_int), ("build_slice_beads", C.c_int),
         ("step_min_blocks", C.c_int), ("step_strategy", C.c_int), ("group_rebuild_pct", C.c_int),
-        ("lean_prep", C.c_int),
+        ("lean_prep", C.c_int), ("queue_wait_ns", C.c_int64), ("stage_wait_ns", C.c_int64),
     ]
 
 
@@ -110,6 +111,8 @@ _PROTOS = {
     "sop_engine_free_bytes": (C.c_int, [VP, C.POINTER(C.c_int64)]),
     "sop_engine_launches": (C.c_int, [VP, C.POINTER(C.c_int64)]),
     "sop_engine_prep_fallbacks": (C.c_int, [VP, C.POINTER(C.c_int64)]),
+    "sop_engine_inject_stall": (C.c_int, [VP, C.c_int64, C.c_int]),
+    "sop_engine_wait_errors": (C.c_int, [VP, IP]),
     "sop_probe_l2_read": (C.c_int, [C.c_int, C.c_int64, C.c_int, C.POINTER(C.c_double)]),
     "sop_replica_add": (C.c_int, [VP, C.POINTER(SystemDesc), IP]),
     "sop_replica_remove": (C.c_int, [VP, C.c_int]),

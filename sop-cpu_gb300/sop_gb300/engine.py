@@ -260,6 +260,19 @@ class Engine:
         L.check(L.lib().sop_engine_prep_fallbacks(self.h, C.byref(n)), "sop_engine_prep_fallbacks")
         return n.value
 
+    def inject_stall(self, publish_delay_ns: int = 0, skip_stage_copy: bool = False):
+        """Diagnostics: stalls that make the device-side waits run out (tests
+        of the timeout path); both zero = normal operation."""
+        L.check(L.lib().sop_engine_inject_stall(self.h, int(publish_delay_ns), int(skip_stage_copy)),
+                "sop_engine_inject_stall")
+
+    def wait_errors(self) -> int:
+        """Waits that ran out in the last call that timed out: bit 0 staging
+        copy, bit 1 work queue."""
+        b = C.c_int()
+        L.check(L.lib().sop_engine_wait_errors(self.h, C.byref(b)), "sop_engine_wait_errors")
+        return b.value
+
     def sync(self):
         L.check(L.lib().sop_engine_sync(self.h), "sop_engine_sync")
 
