@@ -49,16 +49,17 @@ struct Tuner {
     log += buf;
   }
 
-  // S warm-up steps, then S timed steps: milliseconds per step
-  int trial(double* ms_per_step) {
+  // n warm-up steps (default S), then n timed steps: milliseconds per step
+  int trial(double* ms_per_step, int n = 0) {
     NvtxRange range("autotune trial");
+    if (n <= 0) n = S;
     float ms = 0;
-    int rc = run_steps(e, S, nullptr);
+    int rc = run_steps(e, n, nullptr);
     if (rc) return rc;
-    rc = run_steps(e, S, &ms);
+    rc = run_steps(e, n, &ms);
     if (rc) return rc;
-    left -= 2 * (int64_t)S;
-    *ms_per_step = ms / S;
+    left -= 2 * (int64_t)n;
+    *ms_per_step = ms / n;
     return SOP_OK;
   }
 };
@@ -154,8 +155,14 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
   int ntrials = 1;
   if (what & SOP_TUNE_SHAPE)
     for (const Knob& k : knobs) ntrials += (int)k.values.size();
-  for (size_t b = 0; b < buckets.size(); b++) ntrials += (int)(skins.size() + edges.size());
-  Tuner T{e, steps_per_trial, (int64_t)ntrials * 2 * steps_per_trial, std::string()};
+  // list trials span several rebuild intervals, so each lasts at least 400
+  // steps; the bucket's current skin and edge are timed first, and a
+  // candidate replaces them only when 2% faster
+  const int SL = std::max(steps_per_trial, 400);
+  int ltrials = 0;
+  for (size_t b = 0; b < buckets.size(); b++) ltrials += 1 + (int)(skins.size() + edges.size());
+  Tuner T{e, steps_per_trial,
+          (int64_t)ntrials * 2 * steps_per_trial + (int64_t)ltrials * 2 * SL, std::string()};
   const int64_t total = T.left;
   rc = begin_all(e, total);
   if (rc) return rc;
@@ -193,7 +200,14 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
   for (auto& b : buckets) {
     const Replica& R0 = e->reps[b.ids[0]];
     double best_skin = R0.params.skin, best_edge = R0.params.cell_edge, bms = 1e300;
+    rc = set_lists(e, b.ids, best_skin, best_edge);
+    if (rc) return rc;
+    if ((rc = T.trial(&bms, SL))) return rc;
+    used++;
+    T.note("bucket n=[%d,%d) replicas=%zu skin=%.1f edge=%.1f  %.4f ms/step (current)\n", b.lo,
+           b.hi, b.ids.size(), best_skin, best_edge, bms);
     for (double s : skins) {
+      if (s == best_skin) continue;
       rc = set_lists(e, b.ids, s, best_edge);
       if (rc == SOP_ERR_FULL) {  // longer rows than the list arena holds: not a candidate
         T.note("bucket n=[%d,%d) skin=%.1f skipped (list arena full)\n", b.lo, b.hi, s);
@@ -202,21 +216,22 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
       }
       if (rc) return rc;
       double ms = 0;
-      if ((rc = T.trial(&ms))) return rc;
+      if ((rc = T.trial(&ms, SL))) return rc;
       used++;
       T.note("bucket n=[%d,%d) replicas=%zu skin=%.1f edge=%.1f  %.4f ms/step\n", b.lo, b.hi,
              b.ids.size(), s, best_edge, ms);
-      if (ms < bms * 0.99) { bms = ms; best_skin = s; }
+      if (ms < bms * 0.98) { bms = ms; best_skin = s; }
     }
     for (double edge : edges) {
+      if (edge == best_edge) continue;
       rc = set_lists(e, b.ids, best_skin, edge);
       if (rc) return rc;
       double ms = 0;
-      if ((rc = T.trial(&ms))) return rc;
+      if ((rc = T.trial(&ms, SL))) return rc;
       used++;
       T.note("bucket n=[%d,%d) replicas=%zu skin=%.1f edge=%.1f  %.4f ms/step\n", b.lo, b.hi,
              b.ids.size(), best_skin, edge, ms);
-      if (ms < bms * 0.99) { bms = ms; best_edge = edge; }
+      if (ms < bms * 0.98) { bms = ms; best_edge = edge; }
     }
     rc = set_lists(e, b.ids, best_skin, best_edge);
     if (rc) return rc;
