@@ -15,11 +15,13 @@ e2e        the same metric through sop_run_host: every step uploads all
 plain      the plain one-system-per-launch GPU path (no graph, no batching)
            over the same mix, for the batched/plain ratio.
 roofline   the fused step kernel: algorithmic bytes per launch over its
-           CUDA-event duration against MEASURED_PEAKS.json hbm_gbs; traffic
-           = DRAM bytes per launch of the same kernel on the same workload
-           from the ncu capture summarized in profiles/k_step_mix512.md
-           (caches flushed before the captured pass); the same achieved GB/s
-           against the L2 read bandwidth measured in the run.
+           CUDA-event duration against the measured HBM copy bandwidth;
+           traffic = DRAM bytes per launch of the same kernel on the same
+           workload from the recorded ncu capture (caches flushed before the
+           captured pass), or null when the kernel source changed since that
+           capture; the same achieved GB/s against the L2 read bandwidth
+           measured in the run; issue_frac = the kernel's warp instructions
+           (recorded capture) over the SMs' issue slots in its live duration.
 cpu_baseline  the CPU oracle (the reference algorithm restated in C) on a
            stratified sample of the replicas, all host threads.
 served     Poisson arrivals into the continuous-batching server: throughput,
@@ -82,6 +84,8 @@ def parse():
     ap.add_argument("--single-steps", type=int, default=10000,
                     help="single-system leg: steps, in windows of 1000 (0 = skip)")
     ap.add_argument("--large-steps", type=int, default=2000)
+    ap.add_argument("--leg", default="all", choices=["all", "serve", "large", "single"],
+                    help="run one secondary leg alone and print its JSON (no headline line)")
     return ap.parse_args()
 
 
@@ -130,17 +134,43 @@ def default_workload(args):
     return (args.replicas, args.lo, args.hi) == (512, 30, 1500) and args.list_mode == "skin"
 
 
-def read_traffic():
-    """DRAM bytes per k_step launch (read + write) recorded from one ncu
-    capture of the default workload, or None."""
+TRAFFIC_RECORD = os.path.join(ROOT, "profiles", "k_step_mix512.md")
+KERNEL_SOURCE = os.path.join(ROOT, "sop-cpu_gb300", "csrc", "kernels.cu")
+
+
+def blob_hash(path):
+    """git's blob hash of a file (what `git hash-object` prints)."""
+    import hashlib
+    data = open(path, "rb").read()
+    return hashlib.sha1(b"blob %d\0" % len(data) + data).hexdigest()
+
+
+def read_capture():
+    """From the recorded ncu capture of k_step on the default workload: DRAM
+    bytes (read + write) and warp instructions per launch, and the blob hash
+    of the kernel source it was captured from.  Values are None when the
+    record is missing or was captured from another source than the one
+    built here."""
+    rec = {"traffic": None, "warp_instructions": None, "source": None}
     try:
-        with open(os.path.join(ROOT, "profiles", "k_step_mix512.md")) as f:
+        with open(TRAFFIC_RECORD) as f:
             for line in f:
                 if line.startswith("traffic:"):
-                    return int(line.split()[1])
+                    rec["traffic"] = int(line.split()[1])
+                elif line.startswith("warp instructions:"):
+                    rec["warp_instructions"] = int(line.split()[2])
+                elif line.startswith("kernels.cu blob:"):
+                    rec["source"] = line.split()[2]
     except (OSError, ValueError, IndexError):
-        pass
-    return None
+        return rec
+    try:
+        current = blob_hash(KERNEL_SOURCE)
+    except OSError:
+        current = None
+    rec["current"] = current
+    if rec["source"] != current:
+        rec["traffic"] = rec["warp_instructions"] = None
+    return rec
 
 
 def read_peaks():
@@ -264,44 +294,80 @@ PN_PER_KCAL_MOL_A = 69.48
 
 def large_system(args):
     """100 chains x 500 beads in one compact globule (50,000 beads), skin
-    lists: mixed-precision throughput; the same system in FP64 precision
-    (the drift reference): its throughput, the mixed-vs-FP64 force error at
-    the start and how far the total energies drift apart over the run (same
-    seed and noise stream)."""
+    lists, noise on: the mixed-precision run and the FP64-precision run (the
+    drift reference) side by side in one engine, same seed and noise stream.
+    Every --large-steps / 10 steps: each run's mean total energy over the
+    block (20 samples), and the force error of the mixed-precision path
+    against the FP64 path at the FP64 run's current positions (random term
+    off on both).  Throughput of each precision alone over a short window."""
     from sop_gb300 import _lib as L
     from sop_gb300 import systems as S
     from sop_gb300.engine import Engine, make_params
     s = S.synth_globule(3000, args.large_chains, args.large_len)
     n = s.nbead
-    steps, nup = args.large_steps, max(1, args.large_steps // 4)
-    sc = [c if c[1] != "nup" else ("set", "nup", str(nup)) for c in workload_script()]
+    steps = args.large_steps
+    blocks = 10 if steps >= 10 * 20 else 1
+    per = max(1, steps // (blocks * 20))
+    sc = workload_script()
     out = {"workload": "%d chains x %d beads, one globule (%d beads), skin lists, T 0.6"
-                       % (args.large_chains, args.large_len, n), "steps": steps}
-    energies = {}
-    with Engine(0, max_beads=2 * n + 4096, max_replicas=4, max_list_entries=n * 400) as eng:
-        for prec in (L.PREC_MIXED, L.PREC_FP64):
-            key = "fp64" if prec == L.PREC_FP64 else "mixed"
+                       % (args.large_chains, args.large_len, n), "steps": per * 20 * blocks}
+    det = L.TERM_FENE | L.TERM_ANGLE | L.TERM_VDW
+    with Engine(0, max_beads=4 * n + 4096, max_replicas=8, max_list_entries=n * 800) as eng:
+        # throughput of each precision alone
+        for prec, key in ((L.PREC_MIXED, "mixed"), (L.PREC_FP64, "fp64")):
             r = eng.add(s, make_params(sc, seed=31337, list_mode="skin", skin=2.0, precision=prec))
-            if prec == L.PREC_MIXED:
-                f_mixed = eng.force(r)
-            else:
-                f64 = eng.force(r)
-                out["force_rel_err_mixed_vs_fp64"] = float(
-                    np.linalg.norm(f_mixed - f64) / np.linalg.norm(f64))
-            eng.run(20)  # warm
-            trace = []
-            total = 0.0
-            for _ in range(4):
-                eng.run(nup)
-                total += eng.timing()[0]
-                trace.append(float(eng.energy(r)[5]))
-            energies[key] = trace
-            out[key + "_bead_steps_per_s"] = n * 4 * nup / (total / 1e3)
+            eng.run(20)
+            eng.run(1000 if prec == L.PREC_MIXED else 200)
+            t = eng.timing()[0]
+            out[key + "_bead_steps_per_s"] = n * (1000 if prec == L.PREC_MIXED else 200) / (t / 1e3)
             eng.remove(r)
-    e_m, e_d = np.array(energies["mixed"]), np.array(energies["fp64"])
-    out["etot_fp64"] = energies["fp64"]
-    out["etot_mixed"] = energies["mixed"]
-    out["energy_drift_rel_max"] = float(np.max(np.abs(e_m - e_d) / np.abs(e_d)))
+        runs = {key: eng.add(s, make_params(sc, seed=31337, list_mode="skin", skin=2.0, precision=prec))
+                for prec, key in ((L.PREC_MIXED, "mixed"), (L.PREC_FP64, "fp64"))}
+        # probes in an engine of their own, which never steps
+        probes = Engine(0, max_beads=2 * n + 4096, max_replicas=4, max_list_entries=n * 400)
+        probe_m = probes.add(s, make_params(sc, force_terms=det, list_mode="skin", skin=2.0))
+        probe_d = probes.add(s, make_params(sc, force_terms=det, list_mode="skin", skin=2.0,
+                                            precision=L.PREC_FP64))
+
+        def force_error():
+            _, x, _ = eng.state(runs["fp64"])
+            for p in (probe_m, probe_d):
+                probes.set_state(p, x)
+                probes.neighbor_list(p)
+                probes.pair_list(p)
+            fd = probes.force(probe_d)
+            return float(np.linalg.norm(probes.force(probe_m) - fd) / np.linalg.norm(fd))
+
+        ferr = [force_error()]
+        block_mean = {"mixed": [], "fp64": []}
+        block_std = {"mixed": [], "fp64": []}
+        t0 = time.perf_counter()
+        for _ in range(blocks):
+            samples = {"mixed": [], "fp64": []}
+            for _ in range(20):
+                eng.run(per)
+                for key, r in runs.items():
+                    samples[key].append(float(eng.energy(r)[5]))
+            for key in samples:
+                block_mean[key].append(float(np.mean(samples[key])))
+                block_std[key].append(float(np.std(samples[key])))
+            ferr.append(force_error())
+        wall = time.perf_counter() - t0
+        status = {key: eng.status(r)[0] for key, r in runs.items()}
+        probes.close()
+    bm, bd = np.array(block_mean["mixed"]), np.array(block_mean["fp64"])
+    # the block means of the two runs: equal within their spread (the runs
+    # separate chaotically, so single energies differ by thermal noise)
+    se = np.sqrt((np.array(block_std["mixed"]) ** 2 + np.array(block_std["fp64"]) ** 2) / 20)
+    out.update({
+        "force_rel_err_mixed_vs_fp64": ferr, "force_rel_err_max": max(ferr),
+        "check_every_steps": per * 20, "etot_block_mean_mixed": block_mean["mixed"],
+        "etot_block_mean_fp64": block_mean["fp64"],
+        "etot_block_rel_diff_max": float(np.max(np.abs(bm - bd) / np.abs(bd))),
+        "etot_block_diff_over_se_max": float(np.max(np.abs(bm - bd) / np.maximum(se, 1e-30))),
+        "etot_drift_rel_mixed": float((bm[-1] - bm[0]) / abs(bm[0])),
+        "etot_drift_rel_fp64": float((bd[-1] - bd[0]) / abs(bd[0])),
+        "status": status, "wall_s": wall})
     return out
 
 
@@ -353,18 +419,22 @@ def serve_stream(args, rank):
     srv.close()
     lat = np.array([r["finish"] - r["submit"] for r in done])
     svc = np.array([r["finish"] - r["start"] for r in done])
+    que = np.array([r["start"] - r["submit"] for r in done])
     work = sum(r["nbead"] * r["steps"] for r in done)
     span = max(r["finish"] for r in done) - t_start
     offered = float(np.sum(pool_sizes[pick] * steps)) / float(arrivals[-1])
     return {"value": work / span, "unit": UNIT, "requests": len(done), "window_s": float(arrivals[-1]),
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "p50_service_s": float(np.percentile(svc, 50)), "p99_service_s": float(np.percentile(svc, 99)),
+            "p50_queue_s": float(np.percentile(que, 50)), "p99_queue_s": float(np.percentile(que, 99)),
+            "span_s": float(span), "bead_steps": float(work),
             "offered_bead_steps_per_s": offered, "pump_phases_s": phases,
             "errors": int(sum(1 for r in done if r["status"] or r["replica_status"])),
-            "stream": "Poisson %.0f req/s, N log-uniform 30-5000 (pool of %d seeded chains), steps "
-                      "log-uniform %g-%g (the 1e4-1e6 of the serving config scaled by 1/100 so requests "
-                      "complete inside the window), T 0.4-0.9, pull 0-15 pN"
-                      % (args.serve_rate, len(pool), lo, hi)}
+            "stream": "Poisson %.0f req/s for %.0f s, then drained, N log-uniform 30-5000 (pool of %d "
+                      "seeded chains), steps log-uniform %g-%g%s, T 0.4-0.9, pull 0-15 pN"
+                      % (args.serve_rate, args.serve_seconds, len(pool), lo, hi,
+                         "" if (lo, hi) == (1e4, 1e6) else
+                         " (the serving configuration's 1e4-1e6 scaled)")}
 
 
 def force_err(eng, r, s):
@@ -485,6 +555,12 @@ def run_gb300(args):
 
     # roofline of the fused step kernel
     step_ms, pro_ms = eng.profile_steps(md)
+    cap = read_capture() if default_workload(args) else {"traffic": None, "warp_instructions": None}
+    props = torch.cuda.get_device_properties(local)
+    clk_mhz = clk.summary().get("sm_mhz") or 2070.0
+    issue_frac = (cap["warp_instructions"] / (props.multi_processor_count * 4 * clk_mhz * 1e6 *
+                                              step_ms / 1e3)
+                  if cap.get("warp_instructions") else None)
     algo = algorithmic_bytes(eng, ids, systems)
     peak, peak_kind = read_peaks()
     achieved = algo / (step_ms / 1e3) / 1e9
@@ -548,8 +624,11 @@ def run_gb300(args):
         "force_rel_err": ferr,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": read_traffic() if default_workload(args) else None,
-                     "traffic_note": "ncu, caches flushed before the captured pass",
+                     "traffic": cap["traffic"],
+                     "traffic_note": ("ncu, caches flushed before the captured pass; captured from "
+                                      "kernels.cu blob %s, built from %s" % (cap.get("source"),
+                                                                           cap.get("current"))),
+                     "issue_frac": issue_frac,
                      "kernel": "k_step (fused force + Langevin)", "kernel_ms": step_ms,
                      "prologue_ms": pro_ms, "algorithmic_bytes_per_launch": algo,
                      "l2": {"peak": l2_gbs, "frac": achieved / l2_gbs,
@@ -589,6 +668,17 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.leg != "all":
+        import torch
+        torch.cuda.set_device(0)
+        fn = {"serve": lambda: serve_stream(args, 0), "large": lambda: large_system(args),
+              "single": lambda: single_system(args)}[args.leg]
+        with ClockSampler(0) as clk:
+            res = fn()
+        res["leg"] = args.leg
+        res["clocks"] = clk.summary()
+        print(json.dumps(res))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
