@@ -447,6 +447,10 @@ static int fill_repdev(const sop_params& p, RepDev& d) {
   d.boxl = p.boxl;
   d.lcell = p.lcell;
   d.ncell = p.ncell;
+  // the box edge as a two-float, so an image shift k boxl keeps FP32 accuracy
+  d.Lh = (float)p.boxl;
+  d.Ll = (float)(p.boxl - (double)d.Lh);
+  d.invL = (float)(1.0 / p.boxl);
   d.a1 = (float)p.a1; d.a2 = (float)p.a2; d.a3 = (float)p.a3; d.a4 = (float)p.a4;
   d.a1d = p.a1; d.a2d = p.a2; d.a3d = p.a3; d.a4d = p.a4;
   double amp = (p.h > 0 && p.T > 0 && p.zeta > 0) ? std::sqrt(2.0 * p.T * p.zeta / p.h) : 0.0;
@@ -502,6 +506,39 @@ static int max_candidates(const sop_system_desc* d, const std::vector<int>& type
       lo[c] = std::min(lo[c], x[3 * i + c]);
       hi[c] = std::max(hi[c], x[3 * i + c]);
     }
+  const double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+  const double L = d->params.boxl;
+  if (ext + 2.0 * rl >= 0.5 * L) {
+    // minimum images apply (global.cpp:223-227): every pair, as the device
+    // build of such a replica does
+    auto rnd = [](double v) { return v > 0 ? std::floor(v + 0.5) : std::ceil(v - 0.5); };
+    auto img = [&](double v) { return v - L * rnd(v / L); };
+    const double lc = d->params.lcell, nc = d->params.ncell;
+    int best = 0;
+    for (int i = 0; i < n; i++) {
+      int cnt = 0;
+      for (int j = 0; j < n; j++) {
+        if (j == i || (chain[i] == chain[j] && std::abs(i - j) <= 2)) continue;
+        if (mode == SOP_LIST_CELL) {
+          bool adj = true;
+          for (int c = 0; c < 3; c++) {
+            double cd = std::floor(x[3 * i + c] / lc) - std::floor(x[3 * j + c] / lc);
+            cd -= nc * rnd(cd / nc);
+            adj = adj && cd >= -1.0 && cd <= 1.0;
+          }
+          cnt += adj;
+          continue;
+        }
+        const double dx = img(x[3 * j] - x[3 * i]), dy = img(x[3 * j + 1] - x[3 * i + 1]),
+                     dz = img(x[3 * j + 2] - x[3 * i + 2]);
+        const double r = mode == SOP_LIST_SKIN ? 2.5 * T.sigma_rep[type[i]][type[j]] + d->params.skin
+                                               : 3.2 * T.sigma_rep[type[i]][type[j]];
+        cnt += dx * dx + dy * dy + dz * dz < r * r * 1.01;
+      }
+      best = std::max(best, cnt);
+    }
+    return best;
+  }
   long long dim[3];
   for (;;) {
     for (int c = 0; c < 3; c++) dim[c] = (long long)((hi[c] - lo[c]) / edge) + 1;
@@ -1163,7 +1200,10 @@ extern "C" int sop_replica_set_params(sop_engine* e, int r, const sop_params* p)
   rc = fill_repdev(*p, cfg);
   if (rc) return rc;
   Replica& R = e->reps[r];
-  bool mode_changed = cfg.mode != d.mode || p->skin != R.params.skin;
+  // a new list mode or skin, or a new box or cell grid (minimum images are
+  // decided at every build), rebuilds the lists now
+  bool mode_changed = cfg.mode != d.mode || p->skin != R.params.skin || p->boxl != R.params.boxl ||
+                      p->lcell != R.params.lcell || p->ncell != R.params.ncell;
   // another precision moves the replica to the other step kernel's items (the
   // next run restarts from the stored velocities, so no increment carries over)
   if (cfg.prec != d.prec) e->layout_dirty = true;
@@ -1171,6 +1211,7 @@ extern "C" int sop_replica_set_params(sop_engine* e, int r, const sop_params* p)
   d.mode = cfg.mode; d.terms = cfg.terms; d.prec = cfg.prec; d.nnlup = cfg.nnlup; d.nup = cfg.nup;
   d.skin = cfg.skin; d.cell_edge = cfg.cell_edge; d.half_skin2 = cfg.half_skin2;
   d.boxl = cfg.boxl; d.lcell = cfg.lcell; d.ncell = cfg.ncell;
+  d.Lh = cfg.Lh; d.Ll = cfg.Ll; d.invL = cfg.invL;
   d.a1 = cfg.a1; d.a2 = cfg.a2; d.a3 = cfg.a3; d.a4 = cfg.a4;
   d.a1d = cfg.a1d; d.a2d = cfg.a2d; d.a3d = cfg.a3d; d.a4d = cfg.a4d;
   d.noise_amp = cfg.noise_amp; d.T = cfg.T; d.kbnd = cfg.kbnd; d.R0sq = cfg.R0sq;

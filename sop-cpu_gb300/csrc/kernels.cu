@@ -47,17 +47,41 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+__device__ __forceinline__ float rnd_f(float v) { return v > 0.f ? floorf(v + 0.5f) : ceilf(v - 0.5f); }
+
+// A staged difference x_j - x_i in two floats (s + t): s = hj - hi rounded,
+// t = its rounding error plus lj - li.  With IMG, the minimum image: the box
+// shift k Lh comes off s exactly (|s - k Lh| <= boxl/2 is a multiple of the
+// coarser ulp of the two, so the single rounding of the fma is exact) and
+// k Ll off the small part, so an image keeps the accuracy of a plain pair.
+struct BoxF {
+  float Lh, Ll, invL;
+};
+template <bool IMG>
+__device__ __forceinline__ void staged_diff(float hj, float lj, float hi, float lo, const BoxF& B,
+                                            float& s, float& t) {
+  float e;
+  two_sum(hj, -hi, s, e);
+  t = e + (lj - lo);
+  if (IMG) {
+    const float k = rnd_f(s * B.invL);
+    s = fmaf(-k, B.Lh, s);
+    t = fmaf(-k, B.Ll, t);
+  }
+}
+
 // d^2 - r0^2 between two staged beads, in two-float arithmetic (Knuth's
 // TwoSum, Dekker's exact product via FMA), accurate to ~2^-46 of d^2; also
-// returns dx (float, i -> j) and d^2 (float).  r0^2 = r0h + r0l.
+// returns dx (float, i -> j) and d^2 (float).  r0^2 = r0h + r0l.  IMG: the
+// minimum image of the difference (staged_diff).
+template <bool IMG = false>
 __device__ __forceinline__ float d2_minus(const float4& hi, const float4& lo, const float4& hj,
                                           const float4& lj, float r0h, float r0l, float& dx,
-                                          float& dy, float& dz, float& d2) {
-  float sx, ex, sy, ey, sz, ez;
-  two_sum(hj.x, -hi.x, sx, ex);
-  two_sum(hj.y, -hi.y, sy, ey);
-  two_sum(hj.z, -hi.z, sz, ez);
-  const float tx = ex + (lj.x - lo.x), ty = ey + (lj.y - lo.y), tz = ez + (lj.z - lo.z);
+                                          float& dy, float& dz, float& d2, const BoxF& B = BoxF{}) {
+  float sx, tx, sy, ty, sz, tz;
+  staged_diff<IMG>(hj.x, lj.x, hi.x, lo.x, B, sx, tx);
+  staged_diff<IMG>(hj.y, lj.y, hi.y, lo.y, B, sy, ty);
+  staged_diff<IMG>(hj.z, lj.z, hi.z, lo.z, B, sz, tz);
   const float px = sx * sx, py = sy * sy, pz = sz * sz;
   const float pex = fmaf(sx, sx, -px), pey = fmaf(sy, sy, -py), pez = fmaf(sz, sz, -pz);
   float a, ea, bb, eb, c, ec;
@@ -81,6 +105,51 @@ __device__ __forceinline__ double exact_d2(const double* X, long long cap, long 
   double dy = __dsub_rn(X[cap + gj], X[cap + gi]);
   double dz = __dsub_rn(X[2 * cap + gj], X[2 * cap + gi]);
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// The reference's minimum image of one FP64 difference, d - boxl rnd(d/boxl)
+// (global.cpp:223-227, applied to every pair, bond and angle: energy.cpp,
+// neighbor_list.cpp:27-37), in its operation order, no FMA.  The image of -d
+// is minus the image of d (rnd rounds half away from zero), so the direction
+// of the difference does not change d^2.
+__device__ __forceinline__ double image_d(double d, double L) {
+  const double q = __ddiv_rn(d, L);
+  const double k = q > 0.0 ? floor(__dadd_rn(q, 0.5)) : ceil(__dsub_rn(q, 0.5));
+  return __dsub_rn(d, __dmul_rn(L, k));
+}
+
+// exact_d2 with minimum images when L > 0 (replicas in image mode).
+__device__ __forceinline__ double exact_d2i(const double* X, long long cap, long long gi,
+                                            long long gj, double L) {
+  double dx = __dsub_rn(X[gj], X[gi]);
+  double dy = __dsub_rn(X[cap + gj], X[cap + gi]);
+  double dz = __dsub_rn(X[2 * cap + gj], X[2 * cap + gi]);
+  if (L > 0.0) {
+    dx = image_d(dx, L);
+    dy = image_d(dy, L);
+    dz = image_d(dz, L);
+  }
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// The reference's cell-list predicate (cell_list.cpp:24-41): cells
+// floor(x / lcell), their index differences wrapped by ncell, adjacent when
+// every wrapped difference lies in [-1, 1].  For replicas in image mode, whose
+// grid is a single cell.
+__device__ __forceinline__ bool cell_adjacent_ref(const double* X, long long cap, long long gi,
+                                                  long long gj, double lc, double nc) {
+  for (int c = 0; c < 3; c++) {
+    const double ci = floor(__ddiv_rn(X[c * cap + gi], lc));
+    const double cj = floor(__ddiv_rn(X[c * cap + gj], lc));
+    const double cd = image_d(__dsub_rn(ci, cj), nc);
+    if (!(cd >= -1.0 && cd <= 1.0)) return false;
+  }
+  return true;
+}
+
+// FP32 minimum image of a relative-position difference (screens only).
+__device__ __forceinline__ float image_f(float d, float L, float invL) {
+  return fmaf(-rnd_f(d * invL), L, d);
 }
 
 // d2 < rc2, screened in FP32 and re-decided in FP64 inside a relative band.
@@ -232,7 +301,7 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
         m1[c] = fmaxf(m1[c], red[3 + c][w]);
       }
     BinHdr h;
-    h.ok = 0; h.status = 0; h.nx = h.ny = h.nz = 1; h.K = 0; h.ncell = 1;
+    h.ok = 0; h.status = 0; h.img = 0; h.nx = h.ny = h.nz = 1; h.K = 0; h.ncell = 1;
     h.edge = 3.0e38f; h.ox = m0[0]; h.oy = m0[1]; h.oz = m0[2]; h.cx0 = h.cy0 = h.cz0 = 0;
     h.margin = 1e-5f;
     const float rl_max = list_cutoff_max(R, mode);
@@ -244,8 +313,11 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
       h.status = SOP_ST_NONFINITE;
     } else {
       const float ext = fmaxf(m1[0] - m0[0], fmaxf(m1[1] - m0[1], m1[2] - m0[2]));
-      // the minimum image must be the identity for every candidate pair
-      if ((double)ext + 2.0 * rl_max >= 0.5 * R->boxl) h.status |= SOP_ST_PERIODIC;
+      // minimum images (global.cpp:223-227) are the identity for every pair
+      // while the extent stays below half the box by two list cutoffs; past
+      // that, and always in mode none (no later build re-checks it), the
+      // replica runs in image mode
+      h.img = mode == SOP_LIST_NONE || (double)ext + 2.0 * rl_max >= 0.5 * R->boxl;
       // FP32 screening band: relative positions carry ~ext * 2^-24 of error
       if (rl_max > 0.f) h.margin = 1e-5f + 16.0f * ext * 5.9604645e-8f / rl_max;
       const long long ccap = R->cell_cap;
@@ -258,7 +330,7 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
         }
         h.cx0 = c0[0]; h.cy0 = c0[1]; h.cz0 = c0[2];
         h.nx = c1[0] - c0[0] + 1; h.ny = c1[1] - c0[1] + 1; h.nz = c1[2] - c0[2] + 1;
-        if (2.0 * (double)(max(h.nx, max(h.ny, h.nz)) + 1) >= R->ncell) h.status |= SOP_ST_PERIODIC;
+        if (2.0 * (double)(max(h.nx, max(h.ny, h.nz)) + 1) >= R->ncell) h.img = 1;  // cells wrap
         h.edge = (float)lc;
         h.K = 1;
         if ((long long)h.nx * h.ny * h.nz > ccap) h.status |= SOP_ST_GRID;
@@ -280,6 +352,13 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
           e *= 1.25f;
         }
         h.K = e >= rcut ? 1 : 2;
+      }
+      if (h.img) {
+        // every bead a candidate of every other: one cell, decisions with images
+        h.nx = h.ny = h.nz = 1;
+        h.K = 0;
+        h.edge = 3.0e38f;
+        h.status &= ~SOP_ST_GRID;
       }
       h.ncell = h.nx * h.ny * h.nz;
       h.ok = !(h.status & SOP_ST_GRID);
@@ -327,7 +406,9 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
     p.w = u2f(f2u(hq.w) | (f2u(lq.w) << 2));  // type | chain << 2
     A.bin_p[off + i] = p;
     int cx, cy, cz;
-    if (mode == SOP_LIST_CELL) {
+    if (H.img) {
+      cx = cy = cz = 0;
+    } else if (mode == SOP_LIST_CELL) {
       const double lc = R->lcell;
       cx = (int)floor(__ddiv_rn(X[off + i], lc)) - H.cx0;
       cy = (int)floor(__ddiv_rn(X[cap + off + i], lc)) - H.cy0;
@@ -377,7 +458,7 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
   __syncthreads();
 
   // 4. scatter, then bead order inside every cell (deterministic rows)
-  if (mode == SOP_LIST_NONE) {
+  if (mode == SOP_LIST_NONE || H.img) {
     for (int i = tid; i < n; i += nt) sorted[i] = i;
   } else {
     for (int i = tid; i < n; i += nt) {
@@ -405,6 +486,7 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
   }
   if (tid == 0) {
     A.bin_hdr[r] = H;
+    R->img = H.img;
     if (H.status) atomicOr(&R->status, H.status);
   }
 }
@@ -426,6 +508,11 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
   const float4* S = A.stage[src] + 2 * (long long)off;
   const double* X = A.X[src];
   const long long cap = A.cap;
+  // image mode: minimum images in every screen and decision, and in cell
+  // mode the reference's wrapped cell predicate per pair
+  const bool img = H->img != 0;
+  const float Lf = R->Lh, invLf = R->invL;
+  const double Limg = img ? R->boxl : 0.0, lcell = R->lcell, ncellref = R->ncell;
 
   const float4* P = A.bin_p + off;
   const int* sorted = A.bin_sorted + off;
@@ -545,16 +632,24 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
         const int code_j = __float_as_int(pj.w), chj = code_j >> 2;
         tj = code_j & 3;
         pass = j != i && !(chi == chj && abs(i - j) <= 2);
-        const float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
+        float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
+        if (img) {
+          ddx = image_f(ddx, Lf, invLf);
+          ddy = image_f(ddy, Lf, invLf);
+          ddz = image_f(ddz, Lf, invLf);
+        }
         d2 = ddx * ddx + ddy * ddy + ddz * ddz;
       }
       const long long gj = off + j;
       if (pass && mode != SOP_LIST_NONE && mode != SOP_LIST_CELL) {
-        // cell adjacency is the whole predicate in cell mode (cell_list.cpp:86-88)
         const float rl2f = tj == 2 ? rl2f2 : rl2f1;
         pass = d2 <= rl2f * (1.0f + margin) &&
                within(d2, rl2f, margin,
-                      [&] { return exact_d2(X, cap, gi, gj) < H->rl2d[ti][tj == 2]; });
+                      [&] { return exact_d2i(X, cap, gi, gj, Limg) < H->rl2d[ti][tj == 2]; });
+      } else if (pass && mode == SOP_LIST_CELL && img) {
+        // cell adjacency is the whole predicate in cell mode (cell_list.cpp:86-88);
+        // with a single cell it is decided per pair
+        pass = cell_adjacent_ref(X, cap, gi, gj, lcell, ncellref);
       }
       if (pass) {  // natives are listed separately (sorted by partner)
         int lo = 0, hi = nat_cnt;
@@ -573,7 +668,7 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
           inp = true;  // no pair-list filter without a cutoff type
         } else {
           inp = within(d2, tj == 2 ? pl2f2 : pl2f1, margin,
-                       [&] { return exact_d2(X, cap, gi, gj) < H->pl2d[ti][tj == 2]; });
+                       [&] { return exact_d2i(X, cap, gi, gj, Limg) < H->pl2d[ti][tj == 2]; });
         }
       }
       const unsigned m = __ballot_sync(0xffffffffu, pass);
@@ -611,6 +706,11 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
       int j = e.x & (int)kIdx;
       float4 pj = P[j];
       float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
+      if (img) {
+        ddx = image_f(ddx, Lf, invLf);
+        ddy = image_f(ddy, Lf, invLf);
+        ddz = image_f(ddz, Lf, invLf);
+      }
       float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
       const float r0sq = __int_as_float(e.y);  // r0^2 rounded to FP32: the screen's cutoffs
       const long long gj = off + j;
@@ -618,12 +718,16 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
       if (mode == SOP_LIST_NEIGHBOR) {
         nlb = within(d2, 10.24f * r0sq, margin, [&] {
           const double rc = 3.2 * A.nat_r0[tp.x + k];  // neighbor_list.cpp:44-47
-          return exact_d2(X, cap, gi, gj) < rc * rc;
+          return exact_d2i(X, cap, gi, gj, Limg) < rc * rc;
         });
       } else if (mode == SOP_LIST_CELL) {
-        int c2 = cell[j];
-        int jx = c2 % nx, jy = (c2 / nx) % ny, jz = c2 / (nx * ny);
-        nlb = abs(jx - cx) <= 1 && abs(jy - cy) <= 1 && abs(jz - cz) <= 1;
+        if (img) {
+          nlb = cell_adjacent_ref(X, cap, gi, gj, lcell, ncellref);
+        } else {
+          int c2 = cell[j];
+          int jx = c2 % nx, jy = (c2 / nx) % ny, jz = c2 / (nx * ny);
+          nlb = abs(jx - cx) <= 1 && abs(jy - cy) <= 1 && abs(jz - cz) <= 1;
+        }
       } else {
         nlb = true;
       }
@@ -632,7 +736,7 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
       } else if (nlb) {
         plb = within(d2, 6.25f * r0sq, margin, [&] {
           const double rc = 2.5 * A.nat_r0[tp.x + k];  // sop.cpp:504-506
-          return exact_d2(X, cap, gi, gj) < rc * rc;
+          return exact_d2i(X, cap, gi, gj, Limg) < rc * rc;
         });
       } else {
         plb = false;
@@ -952,7 +1056,25 @@ struct ItemCtx {
   int dyn;
   int pull_i, pull_j;
   unsigned seed_lo, seed_hi;
+  int img;        // minimum images apply (the box itself is read per bead)
 };
+
+// The box of an image-mode replica: FP32 two-float for the staged
+// differences, FP64 for the exact decisions (0 = no image).
+struct BoxCtx {
+  BoxF f;
+  double L;
+};
+template <bool IMG>
+__device__ __forceinline__ BoxCtx box_ctx(const DevArrays& A, int r) {
+  BoxCtx b{};
+  if (IMG) {
+    const RepDev* R = &A.rep[r];
+    b.f = BoxF{R->Lh, R->Ll, R->invL};
+    b.L = R->boxl;
+  }
+  return b;
+}
 
 // The step's view of replica r.
 __device__ __forceinline__ ItemCtx load_ctx(const DevArrays& A, int r) {
@@ -964,6 +1086,7 @@ __device__ __forceinline__ ItemCtx load_ctx(const DevArrays& A, int r) {
   C.a1 = R->a1; C.a2 = R->a2; C.a3 = R->a3; C.a4 = R->a4; C.a5 = R->a5; C.dyn = R->dyn;
   C.amp = R->noise_amp; C.T = R->T; C.kbnd = R->kbnd; C.inv_R0sq = R->inv_R0sq; C.fang = R->fang;
   C.half_skin2 = R->half_skin2; C.pull_f = R->pull_f; C.pull_i = R->pull_i;
+  C.img = R->img;
   C.pull_j = R->pull_j; C.seed_lo = R->seed_lo; C.seed_hi = R->seed_hi;
   // a list build of this step that failed (row overflow, grid, periodic
   // image) leaves the replica frozen: no step on incomplete lists
@@ -1017,15 +1140,16 @@ __device__ __forceinline__ BeadRef bead_ref(const ItemCtx& C, const float4* S, i
 // bead b, and its pair-list bit for the next step.  The force vanishes at the
 // native distance, so (r0/d)^12 - (r0/d)^6 is formed from r0^2 - d^2 in
 // two-float arithmetic: with u = r0^2/d^2 - 1, s^3 - 1 = u (u^2 + 3u + 3).
-template <bool ST>
+template <bool ST, bool IMG>
 __device__ __forceinline__ void native_entry(const DevArrays& A, const ItemCtx& C, const float4* S,
                                              const BeadRef& b, int4 e, int k, bool upd,
-                                             FixAcc& acc) {
+                                             FixAcc& acc, const BoxCtx& bx) {
   const int j = e.x & (int)kIdx;
   const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
   const float r0sq = __int_as_float(e.y);
   float dx, dy, dz, d2;
-  const float diff = d2_minus(b.hi, b.lo, hj, lj, r0sq, __int_as_float(e.z), dx, dy, dz, d2);
+  const float diff = d2_minus<IMG>(b.hi, b.lo, hj, lj, r0sq, __int_as_float(e.z), dx, dy, dz, d2,
+                                   bx.f);
   if (e.x & (int)kPL) {
     if (d2 >= (float)kTol * r0sq) {
       const int tj = (int)f2u(hj.w);
@@ -1042,7 +1166,7 @@ __device__ __forceinline__ void native_entry(const DevArrays& A, const ItemCtx& 
     if (e.x & (int)kNL) {
       plb = within(d2, 6.25f * r0sq, kScreenMargin, [&] {
         double rc = 2.5 * A.nat_r0[k], rc2 = rc * rc;
-        return exact_d2(A.X[C.cur], A.cap, b.g, (long long)C.off + j) < rc2;
+        return exact_d2i(A.X[C.cur], A.cap, b.g, (long long)C.off + j, bx.L) < rc2;
       });
     }
     if (plb != ((e.x & (int)kPL) != 0)) A.nat[k].x = e.x ^ (int)kPL;
@@ -1051,15 +1175,32 @@ __device__ __forceinline__ void native_entry(const DevArrays& A, const ItemCtx& 
 
 // Non-native repulsion (energy.cpp:313-350) of list entry e at row slot idx,
 // and its pair-list bit for the next step.
-template <bool ST>
+template <bool IMG>
+__device__ __forceinline__ void pair_delta(const BeadRef& b, const float4& hj, const float4& lj,
+                                           const BoxF& B, float& dx, float& dy, float& dz) {
+  if (!IMG) {
+    dx = (hj.x - b.hi.x) + (lj.x - b.lo.x);
+    dy = (hj.y - b.hi.y) + (lj.y - b.lo.y);
+    dz = (hj.z - b.hi.z) + (lj.z - b.lo.z);
+  } else {
+    float s, t;
+    staged_diff<true>(hj.x, lj.x, b.hi.x, b.lo.x, B, s, t);
+    dx = s + t;
+    staged_diff<true>(hj.y, lj.y, b.hi.y, b.lo.y, B, s, t);
+    dy = s + t;
+    staged_diff<true>(hj.z, lj.z, b.hi.z, b.lo.z, B, s, t);
+    dz = s + t;
+  }
+}
+
+template <bool ST, bool IMG>
 __device__ __forceinline__ void nonnative_entry(const DevArrays& A, const ItemCtx& C, const float4* S,
                                                 const BeadRef& b, int e, long long idx, bool upd,
-                                                FixAcc& acc) {
+                                                FixAcc& acc, const BoxCtx& bx) {
   const int j = e & (int)kIdx;
   const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
-  const float dx = (hj.x - b.hi.x) + (lj.x - b.lo.x);
-  const float dy = (hj.y - b.hi.y) + (lj.y - b.lo.y);
-  const float dz = (hj.z - b.hi.z) + (lj.z - b.lo.z);
+  float dx, dy, dz;
+  pair_delta<IMG>(b, hj, lj, bx.f, dx, dy, dz);
   const float d2 = dx * dx + dy * dy + dz * dz;
   const int tj = (int)f2u(hj.w);
   const float s2 = c_ff.s2[b.ti][tj];
@@ -1073,7 +1214,7 @@ __device__ __forceinline__ void nonnative_entry(const DevArrays& A, const ItemCt
   }
   if (upd) {
     const bool plb = within(d2, c_ff.rc2_pl_f[b.ti][tj], kScreenMargin, [&] {
-      return exact_d2(A.X[C.cur], A.cap, b.g, (long long)C.off + j) < c_ff.rc2_pl[b.ti][tj];
+      return exact_d2i(A.X[C.cur], A.cap, b.g, (long long)C.off + j, bx.L) < c_ff.rc2_pl[b.ti][tj];
     });
     if (plb != ((e & (int)kPL) != 0)) A.nl[idx] = e ^ (int)kPL;
   }
@@ -1082,14 +1223,14 @@ __device__ __forceinline__ void nonnative_entry(const DevArrays& A, const ItemCt
 // FENE (energy.cpp:402-447) of bond record bd; d^2 - r0^2 in two-float
 // arithmetic so the stretch dev = (d^2 - r0^2)/(d + r0) keeps FP32 relative
 // accuracy.
-template <bool ST>
+template <bool ST, bool IMG>
 __device__ __forceinline__ void bond_entry(const ItemCtx& C, const float4* S, const BeadRef& b, int4 bd,
-                                           FixAcc& acc) {
+                                           FixAcc& acc, const BoxCtx& bx) {
   const int j = bd.x;
   const float r0 = __int_as_float(bd.y), r0h = __int_as_float(bd.z), r0l = __int_as_float(bd.w);
   const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
   float dx, dy, dz, d2;
-  const float diff = d2_minus(b.hi, b.lo, hj, lj, r0h, r0l, dx, dy, dz, d2);  // d^2 - r0^2
+  const float diff = d2_minus<IMG>(b.hi, b.lo, hj, lj, r0h, r0l, dx, dy, dz, d2, bx.f);  // d^2 - r0^2
   const float d = sqrtf(d2);
   const float dev = __fdividef(diff, d + r0);
   const float den = 1.0f - dev * dev * C.inv_R0sq;
@@ -1099,13 +1240,12 @@ __device__ __forceinline__ void bond_entry(const ItemCtx& C, const float4* S, co
 }
 
 // i,i+2 soft-sphere repulsion (energy.cpp:354-400) with partner j.
-template <bool ST>
+template <bool ST, bool IMG>
 __device__ __forceinline__ void angle_entry(const ItemCtx& C, const float4* S, const BeadRef& b, int j,
-                                            FixAcc& acc) {
+                                            FixAcc& acc, const BoxCtx& bx) {
   const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
-  const float dx = (hj.x - b.hi.x) + (lj.x - b.lo.x);
-  const float dy = (hj.y - b.hi.y) + (lj.y - b.lo.y);
-  const float dz = (hj.z - b.hi.z) + (lj.z - b.lo.z);
+  float dx, dy, dz;
+  pair_delta<IMG>(b, hj, lj, bx.f, dx, dy, dz);
   const float d2 = dx * dx + dy * dy + dz * dz;
   const float d4 = d2 * d2, d8 = d4 * d4;
   const float co = __fdividef(C.fang, d8);
@@ -1197,11 +1337,13 @@ __device__ __forceinline__ void bead_tail(const DevArrays& A, const ItemCtx& C, 
 
 // One bead on a group of G lanes: each lane takes every G-th native entry,
 // list quad, bond and angle (loaded one iteration ahead), the lanes' exact
-// partial sums are reduced with shuffles and lane 0 updates the bead.
-template <int G, bool ST>
+// partial sums are reduced with shuffles and lane 0 updates the bead.  IMG:
+// the replica is in image mode (minimum images on every difference).
+template <int G, bool ST, bool IMG = false>
 __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, const float4* S,
                                           int i, int lane, unsigned gmask) {
   const BeadRef b = bead_ref<ST>(C, S, i);
+  const BoxCtx bx = box_ctx<IMG>(A, C.r);
   const int4 tp = A.topo[b.g];
   // the non-native row: rows start 32-byte aligned and hold a multiple of 8
   // entries, so a lane reads four entries with one 16-byte load (never past
@@ -1224,7 +1366,7 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
     for (int k = lane; k < nat_cnt; k += G) {
       const int4 e = en;
       if (k + G < nat_cnt) en = A.nat[tp.x + k + G];
-      native_entry<ST>(A, C, S, b, e, tp.x + k, upd, acc);
+      native_entry<ST, IMG>(A, C, S, b, e, tp.x + k, upd, acc, bx);
     }
     for (int q = lane; 4 * q < cnt; q += G) {
       const int4 e4 = e4n;
@@ -1234,7 +1376,7 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
       for (int u = 0; u < 4; u++) {
         const int k = 4 * q + u;
         if (k >= cnt) break;
-        nonnative_entry<ST>(A, C, S, b, ev[u], row + k, upd, acc);
+        nonnative_entry<ST, IMG>(A, C, S, b, ev[u], row + k, upd, acc, bx);
       }
     }
   }
@@ -1242,14 +1384,14 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
     for (int k = lane; k < bnd_cnt; k += G) {
       const int4 bd = bn;
       if (k + G < bnd_cnt) bn = A.bnd[tp.y + k + G];
-      bond_entry<ST>(C, S, b, bd, acc);
+      bond_entry<ST, IMG>(C, S, b, bd, acc, bx);
     }
   }
   if (C.terms & SOP_TERM_ANGLE) {
     for (int k = lane; k < ang_cnt; k += G) {
       const int j = an;
       if (k + G < ang_cnt) an = A.ang[tp.z + k + G];
-      angle_entry<ST>(C, S, b, j, acc);
+      angle_entry<ST, IMG>(C, S, b, j, acc, bx);
     }
   }
   // exact cross-lane sum of the fixed-point partials
@@ -1335,10 +1477,16 @@ __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* i
           return;
         }
         parity ^= 1u;
-        for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, true>(A, C, sst, b, lane, gmask);
+        if (C.img)
+          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, true, true>(A, C, sst, b, lane, gmask);
+        else
+          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, true>(A, C, sst, b, lane, gmask);
       } else {
         const float4* S = A.stage[C.cur] + 2 * (long long)C.off;
-        for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, false>(A, C, S, b, lane, gmask);
+        if (C.img)
+          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, false, true>(A, C, S, b, lane, gmask);
+        else
+          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, false>(A, C, S, b, lane, gmask);
       }
     }
     __syncthreads();
@@ -1367,7 +1515,10 @@ __global__ void __launch_bounds__(256, MB) k_step_w(DevArrays A, const StepItem*
     const ItemCtx C = load_ctx(A, w.r);
     if (C.phase == PH_SKIP) continue;
     const float4* S = A.stage[C.cur] + 2 * (long long)C.off;
-    for (int b = w.b0 + grp; b < w.b1; b += 32 / G) step_bead<G, false>(A, C, S, b, lane, gmask);
+    if (C.img)
+      for (int b = w.b0 + grp; b < w.b1; b += 32 / G) step_bead<G, false, true>(A, C, S, b, lane, gmask);
+    else
+      for (int b = w.b0 + grp; b < w.b1; b += 32 / G) step_bead<G, false>(A, C, S, b, lane, gmask);
   }
   if (l32 == 0) {
     __threadfence();
@@ -1406,11 +1557,25 @@ __device__ void step_bead64(const DevArrays& A, const ItemCtx& C, const RepDev* 
     Fz += fix40(cz);
     mag += fabs(cx) + fabs(cy) + fabs(cz);
   };
+  // the pair difference with the reference's minimum image (raw: without,
+  // for the pulling term, which has no reference counterpart)
+  auto delta_raw = [&](int j, double& dx, double& dy, double& dz) {
+    const long long gj = (long long)C.off + j;
+    dx = __dsub_rn(X[gj], xi);
+    dy = __dsub_rn(X[cap + gj], yi);
+    dz = __dsub_rn(X[2 * cap + gj], zi);
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  };
   auto delta = [&](int j, double& dx, double& dy, double& dz) {
     const long long gj = (long long)C.off + j;
     dx = __dsub_rn(X[gj], xi);
     dy = __dsub_rn(X[cap + gj], yi);
     dz = __dsub_rn(X[2 * cap + gj], zi);
+    if (C.img) {
+      dx = image_d(dx, R->boxl);
+      dy = image_d(dy, R->boxl);
+      dz = image_d(dz, R->boxl);
+    }
     return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
   };
   if (C.terms & SOP_TERM_VDW) {
@@ -1490,7 +1655,7 @@ __device__ void step_bead64(const DevArrays& A, const ItemCtx& C, const RepDev* 
   if (C.pull_f != 0.f && (i == C.pull_i || i == C.pull_j)) {
     const int o = (i == C.pull_i) ? C.pull_j : C.pull_i;
     double ux, uy, uz;
-    const double inv = 1.0 / sqrt(delta(o, ux, uy, uz));
+    const double inv = 1.0 / sqrt(delta_raw(o, ux, uy, uz));
     const double pf = R->pull_fd;
     F[0] -= pf * ux * inv; F[1] -= pf * uy * inv; F[2] -= pf * uz * inv;
   }
@@ -1584,6 +1749,7 @@ __device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b
   const long long cap = A.cap;
   const double* X = A.X[buf];
   const float4* S = A.stage[buf];
+  const double Limg = R->img ? R->boxl : 0.0;  // minimum images (energy.cpp:137-139)
   double eb = 0, ea = 0, eatt = 0;
   long long erep_fx = 0;  // list-ordered sum: exact in fixed point (2^-40 kcal/mol)
   for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
@@ -1595,7 +1761,7 @@ __device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b
       for (int k = 0; k < bnd_cnt; k++) {
         const int j = A.bnd[tp.y + k].x;
         if (j <= i) continue;
-        const double d = sqrt(exact_d2(X, cap, gi, off + j));
+        const double d = sqrt(exact_d2i(X, cap, gi, off + j, Limg));
         const double dev = d - A.bnd_r0[tp.y + k];
         eb += log1p(-dev * dev / R->R0sq_d);
       }
@@ -1603,7 +1769,7 @@ __device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b
       for (int k = 0; k < ang_cnt; k++) {
         const int j = A.ang[tp.z + k];
         if (j <= i) continue;
-        const double d2 = exact_d2(X, cap, gi, off + j);
+        const double d2 = exact_d2i(X, cap, gi, off + j, Limg);
         ea += R->e_ang_coeff / (d2 * d2 * d2);
       }
     if (R->terms & SOP_TERM_VDW) {
@@ -1614,7 +1780,7 @@ __device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b
         const int tj = (int)f2u(S[2 * (off + (long long)j)].w);
         const double r0 = A.nat_r0[tp.x + k];
         const double r2 = r0 * r0, r6 = r2 * r2 * r2, r12 = r6 * r6;
-        const double d2 = exact_d2(X, cap, gi, off + j);
+        const double d2 = exact_d2i(X, cap, gi, off + j, Limg);
         const double d6 = d2 * d2 * d2, d12 = d6 * d6;
         eatt += c_ff.coeff_att[ti][tj] * (r12 / d12) - 2.0 * (r6 / d6);  // energy.cpp:224
       }
@@ -1625,7 +1791,7 @@ __device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b
         const int j = e & (int)kIdx;
         if (j <= i || !(e & (int)kPL)) continue;
         const int tj = (int)f2u(S[2 * (off + (long long)j)].w);
-        const double d2 = exact_d2(X, cap, gi, off + j);
+        const double d2 = exact_d2i(X, cap, gi, off + j, Limg);
         const double d6 = d2 * d2 * d2, d12 = d6 * d6;
         const double ep = c_ff.coeff_rep[ti][tj] * (c_ff.sigma_rep12[ti][tj] / d12 + c_ff.sigma_rep6[ti][tj] / d6);
         erep_fx += __double2ll_rn(ep * 1099511627776.0);  // 2^40
@@ -1668,11 +1834,18 @@ __device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red)
   }
   block_sum(s, 3, red);
   const double mx = s[0] / n, my = s[1] / n, mz = s[2] / n;
+  const double Limg = R->img ? R->boxl : 0.0;
   double q[4] = {0, 0, 0, 0};  // contacts, natives, sum |r - mean|^2, sum v^2
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const long long gi = off + i;
-    const double ax = X[gi] - mx, ay = X[cap + gi] - my, az = X[2 * cap + gi] - mz;
-    q[2] += ax * ax + ay * ay + az * az;
+    if (R->img) {
+      // with images the centroid identity does not hold: the pair sum of
+      // sop.cpp:237-249 itself
+      for (int j = i + 1; j < n; j++) q[2] += exact_d2i(X, cap, gi, off + j, Limg);
+    } else {
+      const double ax = X[gi] - mx, ay = X[cap + gi] - my, az = X[2 * cap + gi] - mz;
+      q[2] += ax * ax + ay * ay + az * az;
+    }
     const double vx = A.vel[gi], vy = A.vel[cap + gi], vz = A.vel[2 * cap + gi];
     q[3] += vx * vx + vy * vy + vz * vz;
     const int4 tp = A.topo[gi];
@@ -1681,7 +1854,7 @@ __device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red)
       const int j = A.nat[tp.x + k].x & (int)kIdx;
       if (j <= i) continue;
       const float r_ij = (float)A.nat_r0[tp.x + k];  // sop.cpp:213 reads r0 into a float
-      const double d = sqrt(exact_d2(X, cap, off + j, gi));
+      const double d = sqrt(exact_d2i(X, cap, off + j, gi, Limg));
       q[1] += 1.0;
       if (d / (double)r_ij < 1.25) q[0] += 1.0;
     }
@@ -1690,10 +1863,11 @@ __device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red)
   if (threadIdx.x == 0) {
     R->obs[1] = q[0];
     R->obs[0] = q[1] > 0 ? q[0] / q[1] : 0.0;
-    R->obs[2] = q[2] / n;  // sum_{i<j} d^2 / N^2 = sum |r - mean|^2 / N
+    // sum_{i<j} d^2 / N^2, without images = sum |r - mean|^2 / N
+    R->obs[2] = R->img ? q[2] / ((double)n * (double)n) : q[2] / n;
     // kinT (sop.cpp:262-279): overdamped from the last increments, kept in vel
     R->obs[3] = (R->dyn == SOP_DYN_OVERDAMPED ? q[3] * R->zeta_2h : q[3]) / (3.0 * n);
-    R->obs[4] = sqrt(exact_d2(X, cap, (long long)off, (long long)off + n - 1));
+    R->obs[4] = sqrt(exact_d2i(X, cap, (long long)off, (long long)off + n - 1, Limg));
   }
 }
 
@@ -1752,18 +1926,25 @@ __global__ void k_pairlist(DevArrays A, int r, int off, int n) {
   const float4 hi = S[2 * i], lo = S[2 * i + 1];
   const int ti = (int)f2u(hi.w);
   const int4 tp = A.topo[gi];
+  const BeadRef b{hi, lo, i, ti, gi};
+  const BoxF box{R->Lh, R->Ll, R->invL};
+  const double Limg = R->img ? R->boxl : 0.0;
+  auto diff = [&](const float4& hj, const float4& lj, float& dx, float& dy, float& dz) {
+    if (R->img) pair_delta<true>(b, hj, lj, box, dx, dy, dz);
+    else pair_delta<false>(b, hj, lj, box, dx, dy, dz);
+  };
   const int nat_cnt = tp.w & 0xFFFF;
   for (int k = 0; k < nat_cnt; k++) {
     const int4 e = A.nat[tp.x + k];
     const int j = e.x & (int)kIdx;
     const float4 hj = S[2 * j], lj = S[2 * j + 1];
-    const float dx = (hj.x - hi.x) + (lj.x - lo.x), dy = (hj.y - hi.y) + (lj.y - lo.y),
-                dz = (hj.z - hi.z) + (lj.z - lo.z);
+    float dx, dy, dz;
+    diff(hj, lj, dx, dy, dz);
     const float d2 = dx * dx + dy * dy + dz * dz;
     bool plb = false;
     if (e.x & (int)kNL) {
       const double rc = 2.5 * A.nat_r0[tp.x + k], rc2 = rc * rc;
-      plb = within(d2, (float)rc2, kScreenMargin, [&] { return exact_d2(X, cap, gi, off + j) < rc2; });
+      plb = within(d2, (float)rc2, kScreenMargin, [&] { return exact_d2i(X, cap, gi, off + j, Limg) < rc2; });
     }
     A.nat[tp.x + k].x = (e.x & ~(int)kPL) | (plb ? (int)kPL : 0);
   }
@@ -1773,13 +1954,13 @@ __global__ void k_pairlist(DevArrays A, int r, int off, int n) {
     const int e = A.nl[row + k];
     const int j = e & (int)kIdx;
     const float4 hj = S[2 * j], lj = S[2 * j + 1];
-    const float dx = (hj.x - hi.x) + (lj.x - lo.x), dy = (hj.y - hi.y) + (lj.y - lo.y),
-                dz = (hj.z - hi.z) + (lj.z - lo.z);
+    float dx, dy, dz;
+    diff(hj, lj, dx, dy, dz);
     const float d2 = dx * dx + dy * dy + dz * dz;
     const int tj = (int)f2u(hj.w);
     const double rc2 = c_ff.rc2_pl[ti][tj];
     const bool plb = within(d2, c_ff.rc2_pl_f[ti][tj], kScreenMargin,
-                            [&] { return exact_d2(X, cap, gi, off + j) < rc2; });
+                            [&] { return exact_d2i(X, cap, gi, off + j, Limg) < rc2; });
     A.nl[row + k] = (e & ~(int)kPL) | (plb ? (int)kPL : 0);
   }
 }

@@ -68,6 +68,7 @@ struct DevArrays {
 // Grid of one replica's last binning.
 struct BinHdr {
   int ok, status, nx, ny, nz, K, ncell;  // K: stencil half-width in cells
+  int img;                               // minimum images: one cell, every bead a candidate
   float edge, ox, oy, oz, margin;        // margin: relative FP32 screening band
   int cx0, cy0, cz0;                     // cell-mode origin cell (floor(x / lcell))
   // non-native list and pair cutoffs^2 by [bead type][partner type 1, 2], in

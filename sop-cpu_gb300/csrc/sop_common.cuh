@@ -57,6 +57,9 @@ struct RepDev {
   float cell_edge;         // grid edge for the list build (0 = auto)
   float half_skin2;        // (skin/2)^2
   double boxl, lcell, ncell;
+  float Lh, Ll, invL;      // boxl as a two-float (Lh + Ll) and 1/boxl, for images in FP32
+  int img;                 // minimum images apply (set at each list build, always in
+                           // mode NONE): extent + 2 list cutoffs reached boxl/2
   float a1, a2, a3, a4;    // FP32 integrator constants
   double a1d, a2d, a3d, a4d;
   float noise_amp;         // sqrt(2 T zeta / h)

@@ -24,12 +24,13 @@ GOLDEN_TYPED = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden"
 needs_ref = pytest.mark.skipif(not O.ref_available(), reason="reference tree not built here")
 
 
-def golden_script(mode="neighborlist", temp="0.6", nstep=100, nup=50, dynamics=None):
+def golden_script(mode="neighborlist", temp="0.6", nstep=100, nup=50, dynamics=None, boxl="500",
+                  ncell="62.5"):
     pre = [("set", "dynamics", dynamics)] if dynamics else []
     return pre + [("set", "zeta", "50"), ("set", "t_step", "0.05"), ("set", "temp", temp),
             ("set", "nstep", str(nstep)), ("set", "nup", str(nup)),
-            ("set", "cutofftype", mode), ("set", "nnlup", "10"), ("set", "boxl", "500"),
-            ("set", "ncell", "62.5"), ("set", "run", "1")]
+            ("set", "cutofftype", mode), ("set", "nnlup", "10"), ("set", "boxl", boxl),
+            ("set", "ncell", ncell), ("set", "run", "1")]
 
 
 def system_from_golden(g):
@@ -163,6 +164,48 @@ def test_port_equals_reference_types_and_exclusions(n, mode, frac):
             assert ref.energy(k) == p.energy(k)
         for k in range(4):
             np.testing.assert_array_equal(pairs(ref, k), pairs(p, k))
+
+
+@needs_ref
+@pytest.mark.parametrize("n,mode,boxl,ncell", [(150, "neighborlist", "40", "5"),
+                                               (150, "celllist", "40", "5"),
+                                               (120, "none", "35", "4.375"),
+                                               (300, "neighborlist", "47.5", "5.9375")])
+def test_port_equals_reference_with_periodic_images(n, mode, boxl, ncell):
+    """A box smaller than twice the chain's extent: the minimum image
+    (global.cpp:223-227) applies to list decisions, forces, energies and
+    observables, and the cell list wraps by ncell.  Restatement and reference
+    agree bit for bit."""
+    system = S.synth_chain(6400 + n, n)
+    ext = (system.xyz.max(0) - system.xyz.min(0)).max()
+    assert ext > 0.5 * float(boxl)  # images do apply
+    scr = golden_script(mode, dynamics="underdamped", boxl=boxl, ncell=ncell)
+    ref, port = O.Ref(), O.Port()
+    with tempfile.TemporaryDirectory() as d:
+        path = S.write_reference_files(system, d, scr, run=False)
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            ref.load_script(path)
+            port.load_script(path)
+        finally:
+            os.chdir(cwd)
+    for o in (ref, port):
+        o.set_force_terms(0, 1, 1, 1)
+        o.setup(True)
+    for k in range(4):
+        np.testing.assert_array_equal(pairs(ref, k), pairs(port, k))
+    np.testing.assert_array_equal(ref.energies(), port.energies())
+    np.testing.assert_array_equal(ref.coords(3), port.coords(3))
+    for o in (ref, port):
+        o.run(60)
+        o.energy_eval()
+        o.observables()
+    for which in (1, 2):
+        np.testing.assert_array_equal(ref.coords(which), port.coords(which))
+    np.testing.assert_array_equal(ref.energies(), port.energies())
+    for k in ("Q", "rgsq", "kinT"):
+        assert ref.energy(k) == port.energy(k)
 
 
 def test_typed_system_files_hold_what_the_system_says():
