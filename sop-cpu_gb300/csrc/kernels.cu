@@ -1408,88 +1408,149 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   bead_tail<ST>(A, C, S, b, Fx, Fy, Fz, st);
 }
 
+// Replica segments a step-kernel CTA stages at once (see k_step).
+constexpr int kStepSegs = 16;
+
+__device__ __forceinline__ uint32_t dynamic_smem_bytes() {
+  uint32_t b;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(b));
+  return b;
+}
+
+// Wait for the staging copies of this CTA's mbarrier phase, bounded.  On
+// running out (never expected) it records the fact, lets the copies in flight
+// land in this CTA's shared memory (bounded) and returns false for the whole
+// CTA, which then leaves the step.
+__device__ __forceinline__ bool wait_staged(const DevArrays& A, unsigned long long* mbar,
+                                            uint32_t parity) {
+  const unsigned long long t0 = globaltimer_ns();
+  bool late = false;
+  while (!mbar_try_wait(mbar, parity)) {
+    if (globaltimer_ns() - t0 > (unsigned long long)A.stage_wait_ns) {
+      late = true;
+      break;
+    }
+  }
+  if (__syncthreads_or(late)) {
+    if (threadIdx.x == 0) atomicOr(A.err, 1);
+    const unsigned long long t1 = globaltimer_ns();
+    while (!mbar_try_wait(mbar, parity) && globaltimer_ns() - t1 < kDrainNs) {
+    }
+    return false;
+  }
+  return true;
+}
+
+// Bulk copies of replica C's staged positions into shared memory at dst,
+// counted on mbar (the caller has set the phase's expected bytes).
+__device__ __forceinline__ void stage_replica(const DevArrays& A, const ItemCtx& C, float4* dst,
+                                              unsigned long long* mbar) {
+  if (A.skip_stage_copy) return;  // (diagnostics: expected but not issued)
+  const char* src = reinterpret_cast<const char*>(A.stage[C.cur] + 2 * (long long)C.off);
+  const uint32_t bytes = (uint32_t)C.n * 32u;
+  for (uint32_t o = 0; o < bytes; o += 32768u) {
+    const uint32_t b = (bytes - o < 32768u) ? bytes - o : 32768u;
+    tma_bulk_g2s(reinterpret_cast<char*>(dst) + o, src + o, b, mbar);
+  }
+}
+
+template <int G, bool ST>
+__device__ __forceinline__ void step_bead_any(const DevArrays& A, const ItemCtx& C, const float4* S,
+                                              int b, int lane, unsigned gmask) {
+  if (C.img) step_bead<G, ST, true>(A, C, S, b, lane, gmask);
+  else step_bead<G, ST>(A, C, S, b, lane, gmask);
+}
+
 // TPB: largest block size (256, or 512 for the wide variants); MB: resident
-// CTAs of TPB threads per SM the register allocation is sized for
+// CTAs of TPB threads per SM the register allocation is sized for.
+//
+// Each CTA takes a contiguous block of work items and steps it in rounds.  A
+// round is as many consecutive items as fit in the CTA's shared-memory stage
+// together -- consecutive items of one replica form one segment, and every
+// segment's whole replica is staged once, all of a round's bulk copies on one
+// mbarrier phase -- and its lane groups take beads one at a time from a CTA
+// counter across all of the round's segments: a group that finishes a short
+// row goes on to the next bead of any segment, and the only barrier is the
+// one between rounds (before the stage is refilled).  Every bead's
+// arithmetic is the same whatever the rounds.
 template <int G, int MB, int TPB = 256>
 __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* items,
                                                  const int* nitems_dev, int nitems_host) {
   const int nitems = nitems_dev ? *nitems_dev : nitems_host;
   extern __shared__ __align__(128) float4 sst[];
   __shared__ __align__(8) unsigned long long mbar;
-  __shared__ ItemCtx sC;
+  __shared__ ItemCtx sC[kStepSegs];
+  __shared__ int s_b0[kStepSegs], s_pre[kStepSegs + 1], s_soff[kStepSegs];
+  __shared__ int s_nseg, s_it, s_next, s_wait;
   const int lane = threadIdx.x & (G - 1);
-  const int grp = threadIdx.x / G, ngrp = blockDim.x / G;
   const unsigned gmask =
       (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+  const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int it_end = min(nitems, ((int)blockIdx.x + 1) * per);
   if (threadIdx.x == 0) mbar_init(&mbar, 1);
   fence_async_smem();
   __syncthreads();
   uint32_t parity = 0;
-  // a contiguous block of items per CTA; consecutive items of one replica
-  // merge into one bead range, staged once, with no barrier inside it.  (A
-  // CTA's time is set by its chain of items, each with a fixed staging and
-  // row-latency cost, so equal item counts balance better than equal beads.)
-  const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int it_end = min(nitems, ((int)blockIdx.x + 1) * per);
   for (int it = (int)blockIdx.x * per; it < it_end;) {
-    StepItem w = items[it];
-    int nx = it + 1;
-    for (; nx < it_end; ++nx) {
-      const StepItem v = items[nx];
-      if (v.r != w.r) break;
-      w.b1 = v.b1;
-    }
-    it = nx;
     if (threadIdx.x == 0) {
-      const ItemCtx C = load_ctx(A, w.r);
-      sC = C;
-      if (C.phase != PH_SKIP && w.staged) {
-        const char* src = reinterpret_cast<const char*>(A.stage[C.cur] + 2 * (long long)C.off);
-        const uint32_t bytes = (uint32_t)C.n * 32u;
+      // the round: segments while their replicas fit in the stage together
+      const int cap4 = ((int)dynamic_smem_bytes() - 128) / 16;
+      int ns = 0, off = 0, pre = 0, last_r = -1, b1 = 0;
+      while (it < it_end) {
+        const StepItem w = items[it];
+        if (w.r == last_r) {  // the next item of the segment's replica
+          b1 = w.b1;
+          it++;
+          continue;
+        }
+        if (ns == kStepSegs) break;
+        const ItemCtx C = load_ctx(A, w.r);
+        const int need = (C.phase != PH_SKIP && w.staged) ? 2 * C.n : 0;
+        if (ns > 0 && off + need > cap4) break;
+        if (ns > 0) pre += b1 - s_b0[ns - 1];
+        sC[ns] = C;
+        s_b0[ns] = w.b0;
+        s_pre[ns] = pre;
+        s_soff[ns] = need ? off : -1;
+        off += need;
+        last_r = w.r;
+        b1 = w.b1;
+        ns++;
+        it++;
+      }
+      s_pre[ns] = pre + b1 - s_b0[ns - 1];
+      s_nseg = ns;
+      s_it = it;
+      s_next = 0;
+      s_wait = off > 0;
+      if (off > 0) {
         fence_async_smem();
-        mbar_expect_tx(&mbar, bytes);
-        if (!A.skip_stage_copy)  // (diagnostics: expected but not issued)
-          for (uint32_t o = 0; o < bytes; o += 32768u) {
-            const uint32_t b = (bytes - o < 32768u) ? bytes - o : 32768u;
-            tma_bulk_g2s(reinterpret_cast<char*>(sst) + o, src + o, b, &mbar);
-          }
+        mbar_expect_tx(&mbar, (uint32_t)off * 16u);
+        for (int k = 0; k < ns; k++)
+          if (s_soff[k] >= 0) stage_replica(A, sC[k], sst + s_soff[k], &mbar);
       }
     }
     __syncthreads();
-    const ItemCtx C = sC;
-    if (C.phase != PH_SKIP) {
-      if (w.staged) {
-        const unsigned long long t0 = globaltimer_ns();
-        bool late = false;
-        while (!mbar_try_wait(&mbar, parity)) {
-          if (globaltimer_ns() - t0 > (unsigned long long)A.stage_wait_ns) {
-            late = true;
-            break;
-          }
-        }
-        if (__syncthreads_or(late)) {
-          // never expected: record it, let the copy in flight land in this
-          // CTA's shared memory (bounded), and leave the step
-          if (threadIdx.x == 0) atomicOr(A.err, 1);
-          const unsigned long long t1 = globaltimer_ns();
-          while (!mbar_try_wait(&mbar, parity) && globaltimer_ns() - t1 < kDrainNs) {
-          }
-          return;
-        }
-        parity ^= 1u;
-        if (C.img)
-          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, true, true>(A, C, sst, b, lane, gmask);
-        else
-          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, true>(A, C, sst, b, lane, gmask);
-      } else {
-        const float4* S = A.stage[C.cur] + 2 * (long long)C.off;
-        if (C.img)
-          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, false, true>(A, C, S, b, lane, gmask);
-        else
-          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, false>(A, C, S, b, lane, gmask);
-      }
+    it = s_it;
+    const int nseg = s_nseg, total = s_pre[nseg];
+    if (s_wait) {
+      if (!wait_staged(A, &mbar, parity)) return;
+      parity ^= 1u;
     }
-    __syncthreads();
+    for (;;) {
+      int g = 0;
+      if (lane == 0) g = atomicAdd(&s_next, 1);
+      g = __shfl_sync(gmask, g, 0, G);
+      if (g >= total) break;
+      int k = 0;
+      while (k + 1 < nseg && g >= s_pre[k + 1]) k++;
+      const ItemCtx& C = sC[k];
+      if (C.phase == PH_SKIP) continue;
+      const int b = s_b0[k] + (g - s_pre[k]);
+      if (s_soff[k] >= 0) step_bead_any<G, true>(A, C, sst + s_soff[k], b, lane, gmask);
+      else step_bead_any<G, false>(A, C, A.stage[C.cur] + 2 * (long long)C.off, b, lane, gmask);
+    }
+    __syncthreads();  // the round's beads are done before the stage is refilled
   }
 }
 
