@@ -42,12 +42,18 @@ extern "C" {
 #define SOP_ERR_FULL -9        /* no room: admission refused, retry later        */
 #define SOP_ERR_TIMEOUT -10    /* a bounded device-side wait ran out; the replicas
                                   stepped in that call are in an undefined state */
+#define SOP_ERR_INDEX -11      /* checked build (libsopgpu_checked.so): a list,
+                                  bin, native, bond or angle entry named a bead
+                                  outside its replica; the entry was skipped and
+                                  the stepped replicas are in an undefined state */
 
 /* per-replica status bits (sop_replica_status) */
 #define SOP_ST_NONFINITE 0x1     /* NaN/inf force or position                   */
 #define SOP_ST_FENE 0x2          /* a bond stretched to |d - r0| >= R0           */
 #define SOP_ST_LIST_OVERFLOW 0x4 /* a neighbor-list row overflowed; frozen       */
-#define SOP_ST_PERIODIC 0x8      /* extent reached boxl/2: images would apply    */
+#define SOP_ST_PERIODIC 0x8      /* reserved: no longer raised (a replica whose
+                                    extent reaches boxl/2 steps with minimum
+                                    images, global.cpp:223-227)                 */
 #define SOP_ST_GRID 0x10         /* cell grid larger than the engine supports    */
 
 /* list modes: which pair search feeds the per-step pair-list filter */
@@ -387,8 +393,8 @@ int sop_synth_globule(uint64_t seed, int nchain, int chain_len, int compact_step
  * Result: the engine's non-native neighbor list of the system, the set
  * sop_update_neighbor_list + sop_get_pair_list(which=1) give: pairs on
  * different chains or |i-j| > 2 apart, not native, with d^2 < (3.2 sigma)^2
- * in FP64, open boundaries (no minimum image; the engine flags a replica
- * whose extent would need one with SOP_ST_PERIODIC).  nbead >
+ * in FP64, open boundaries (no box and no minimum image: a system that
+ * needs images, extent near half its box, belongs in the engine).  nbead >
  * SOP_NOALLOC_MAX_BEADS returns SOP_ERR_UNSUPPORTED.  The first call on a
  * device looks up the scratch address there; make it before any stream
  * capture.  Calls share the scratch: calls that overlap on the GPU

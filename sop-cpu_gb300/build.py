@@ -1,4 +1,6 @@
-"""Build libsopgpu.so (and the drop-in program sop_gpu.x) in-tree for sm_103a.
+"""Build libsopgpu.so (and the drop-in program sop_gpu.x) in-tree for sm_103a,
+and libsopgpu_checked.so: the same library with the kernels' partner-index
+checks compiled in (-DSOP_CHECKED; a bad index is reported as SOP_ERR_INDEX).
 
     python sop-cpu_gb300/build.py            # library + program
     python sop-cpu_gb300/build.py --check    # also print -Xptxas -v resource usage
@@ -65,6 +67,12 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> str:
             if verbose_ptxas:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)
+    # the checked kernels (bounds checks on every partner index)
+    checked_obj = os.path.join(BUILD, "kernels_checked.o")
+    if force or verbose_ptxas or _stale(checked_obj, [os.path.join(HERE, "csrc/kernels.cu")] + headers):
+        jobs.append([nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                                     "-Xcompiler", "-ffp-contract=off", "-DSOP_CHECKED", "-c",
+                                     "csrc/kernels.cu", "-o", checked_obj])
     for src in CXX_SOURCES:
         obj = os.path.join(BUILD, os.path.basename(src).replace(".cpp", ".o"))
         objs.append(obj)
@@ -78,6 +86,10 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> str:
     lib = os.path.join(LIBDIR, "libsopgpu.so")
     if force or _stale(lib, objs):
         _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
+    lib_checked = os.path.join(LIBDIR, "libsopgpu_checked.so")
+    objs_checked = [checked_obj if o.endswith(os.sep + "kernels.o") else o for o in objs]
+    if force or _stale(lib_checked, objs_checked):
+        _run([nvcc] + ARCH + ["-shared", "-o", lib_checked] + objs_checked + ["-lcudart"])
     prog_src = os.path.join(HERE, PROGRAM)
     if os.path.exists(prog_src):
         prog = os.path.join(LIBDIR, "sop_gpu.x")

@@ -138,6 +138,7 @@ extern "C" const char* sop_status_string(int s) {
     case SOP_ERR_REPLICA: return "replica error status";
     case SOP_ERR_FULL: return "engine full";
     case SOP_ERR_TIMEOUT: return "a bounded device-side wait ran out";
+    case SOP_ERR_INDEX: return "an index outside its replica (checked build)";
     default: return "unknown";
   }
 }
@@ -1426,9 +1427,10 @@ __global__ void k_set_phase(RepDev* rep, int r, int phase) {
   R->out = 0;
 }
 
-// A bounded device wait ran out (error word `err`, already read back):
-// remember which, clear the word and the work queue (a unit published after
-// its consumer gave up would otherwise be taken by the next step), and report.
+// A bounded device wait ran out, or a checked build found a bad index (error
+// word `err`, already read back): remember which, clear the word and the work
+// queue (a unit published after its consumer gave up would otherwise be taken
+// by the next step), and report.
 static int timed_out(sop_engine* e, int err) {
   e->wait_errors = err;
   CK(cudaMemsetAsync(e->A.err, 0, sizeof(int), e->stream));
@@ -1446,7 +1448,10 @@ static int check_errors(sop_engine* e) {
   int err = 0;
   CK(cudaMemcpyAsync(&err, e->A.err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
   CK(cudaStreamSynchronize(e->stream));
-  return err ? timed_out(e, err) : SOP_OK;
+  if (!err) return SOP_OK;
+  const int rc = timed_out(e, err);
+  // a checked build found a partner index outside its replica
+  return (err & kErrIndex) ? SOP_ERR_INDEX : rc;
 }
 
 extern "C" int sop_engine_inject_stall(sop_engine* e, int64_t publish_delay_ns, int skip_stage_copy) {

@@ -41,6 +41,24 @@ void upload_tables(const FFTables& t, cudaStream_t s) {
 // ---------------------------------------------------------------------------------
 // small helpers
 
+// Checked build (-DSOP_CHECKED): every partner index read from a list row,
+// cell bin, native, bond or angle record is tested against its replica's
+// bead range before the gather; one outside it is recorded in the engine's
+// error word (kErrIndex, reported by the call as SOP_ERR_INDEX) and the entry
+// is skipped.  compute-sanitizer is not available on the GPUs this engine is
+// tested on, so this build stands in for its bounds checks.  The default
+// build compiles the checks out.
+#ifdef SOP_CHECKED
+__device__ __forceinline__ bool gather_ok(const DevArrays& A, int j, int n) {
+  if ((unsigned)j < (unsigned)n) return true;
+  atomicOr(A.err, kErrIndex);
+  return false;
+}
+#define SOP_GATHER_OK(A, j, n) gather_ok((A), (j), (n))
+#else
+#define SOP_GATHER_OK(A, j, n) true
+#endif
+
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
   float bb = s - a;
@@ -496,6 +514,7 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
 // `dyn_bytes`, else read from global memory (L2).  The lanes test 32
 // stencil candidates at a time and ballot-compact the survivors, so each row
 // holds its partners in stencil order, bead order within a cell.
+template <bool IMG>
 __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0, int b1,
                             BuildSmem& B, unsigned char* dyn, int dyn_bytes) {
   RepDev* R = &A.rep[r];
@@ -510,9 +529,9 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
   const long long cap = A.cap;
   // image mode: minimum images in every screen and decision, and in cell
   // mode the reference's wrapped cell predicate per pair
-  const bool img = H->img != 0;
+  const bool img = IMG;  // (the caller dispatches on the replica's binning)
   const float Lf = R->Lh, invLf = R->invL;
-  const double Limg = img ? R->boxl : 0.0, lcell = R->lcell, ncellref = R->ncell;
+  const double Limg = IMG ? R->boxl : 0.0, lcell = R->lcell, ncellref = R->ncell;
 
   const float4* P = A.bin_p + off;
   const int* sorted = A.bin_sorted + off;
@@ -627,7 +646,9 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
       int j = 0, tj = 1;
       float d2 = 0.f;
       if (pass) {
-        j = sorted[segoff + f];
+        const int slot = segoff + f;
+        j = SOP_GATHER_OK(A, slot, n) ? sorted[slot] : i;
+        if (!SOP_GATHER_OK(A, j, n)) j = i;  // (dropped below)
         const float4 pj = P[j];
         const int code_j = __float_as_int(pj.w), chj = code_j >> 2;
         tj = code_j & 3;
@@ -704,6 +725,7 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
     for (int k = lane; k < nat_cnt; k += 32) {
       int4 e = A.nat[tp.x + k];
       int j = e.x & (int)kIdx;
+      if (!SOP_GATHER_OK(A, j, n)) continue;
       float4 pj = P[j];
       float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
       if (img) {
@@ -883,7 +905,8 @@ __device__ void run_unit(const DevArrays& A, int4 w, BuildSmem& B, unsigned char
     const int sb = A.slice_beads;
     const int n = R->n, nsl = (n + sb - 1) / sb;
     const int b0 = w.z * sb, b1 = min(n, b0 + sb);
-    build_slice(A, r, w.w, mode, b0, b1, B, dyn, dyn_bytes);
+    if (A.bin_hdr[r].img) build_slice<true>(A, r, w.w, mode, b0, b1, B, dyn, dyn_bytes);
+    else build_slice<false>(A, r, w.w, mode, b0, b1, B, dyn, dyn_bytes);
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
@@ -1145,6 +1168,7 @@ __device__ __forceinline__ void native_entry(const DevArrays& A, const ItemCtx& 
                                              const BeadRef& b, int4 e, int k, bool upd,
                                              FixAcc& acc, const BoxCtx& bx) {
   const int j = e.x & (int)kIdx;
+  if (!SOP_GATHER_OK(A, j, C.n)) return;
   const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
   const float r0sq = __int_as_float(e.y);
   float dx, dy, dz, d2;
@@ -1198,6 +1222,7 @@ __device__ __forceinline__ void nonnative_entry(const DevArrays& A, const ItemCt
                                                 const BeadRef& b, int e, long long idx, bool upd,
                                                 FixAcc& acc, const BoxCtx& bx) {
   const int j = e & (int)kIdx;
+  if (!SOP_GATHER_OK(A, j, C.n)) return;
   const float4 hj = ldp<ST>(S, 2 * j), lj = ldp<ST>(S, 2 * j + 1);
   float dx, dy, dz;
   pair_delta<IMG>(b, hj, lj, bx.f, dx, dy, dz);
@@ -1384,14 +1409,14 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
     for (int k = lane; k < bnd_cnt; k += G) {
       const int4 bd = bn;
       if (k + G < bnd_cnt) bn = A.bnd[tp.y + k + G];
-      bond_entry<ST, IMG>(C, S, b, bd, acc, bx);
+      if (SOP_GATHER_OK(A, bd.x, C.n)) bond_entry<ST, IMG>(C, S, b, bd, acc, bx);
     }
   }
   if (C.terms & SOP_TERM_ANGLE) {
     for (int k = lane; k < ang_cnt; k += G) {
       const int j = an;
       if (k + G < ang_cnt) an = A.ang[tp.z + k + G];
-      angle_entry<ST, IMG>(C, S, b, j, acc, bx);
+      if (SOP_GATHER_OK(A, j, C.n)) angle_entry<ST, IMG>(C, S, b, j, acc, bx);
     }
   }
   // exact cross-lane sum of the fixed-point partials
@@ -1408,149 +1433,88 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   bead_tail<ST>(A, C, S, b, Fx, Fy, Fz, st);
 }
 
-// Replica segments a step-kernel CTA stages at once (see k_step).
-constexpr int kStepSegs = 16;
-
-__device__ __forceinline__ uint32_t dynamic_smem_bytes() {
-  uint32_t b;
-  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(b));
-  return b;
-}
-
-// Wait for the staging copies of this CTA's mbarrier phase, bounded.  On
-// running out (never expected) it records the fact, lets the copies in flight
-// land in this CTA's shared memory (bounded) and returns false for the whole
-// CTA, which then leaves the step.
-__device__ __forceinline__ bool wait_staged(const DevArrays& A, unsigned long long* mbar,
-                                            uint32_t parity) {
-  const unsigned long long t0 = globaltimer_ns();
-  bool late = false;
-  while (!mbar_try_wait(mbar, parity)) {
-    if (globaltimer_ns() - t0 > (unsigned long long)A.stage_wait_ns) {
-      late = true;
-      break;
-    }
-  }
-  if (__syncthreads_or(late)) {
-    if (threadIdx.x == 0) atomicOr(A.err, 1);
-    const unsigned long long t1 = globaltimer_ns();
-    while (!mbar_try_wait(mbar, parity) && globaltimer_ns() - t1 < kDrainNs) {
-    }
-    return false;
-  }
-  return true;
-}
-
-// Bulk copies of replica C's staged positions into shared memory at dst,
-// counted on mbar (the caller has set the phase's expected bytes).
-__device__ __forceinline__ void stage_replica(const DevArrays& A, const ItemCtx& C, float4* dst,
-                                              unsigned long long* mbar) {
-  if (A.skip_stage_copy) return;  // (diagnostics: expected but not issued)
-  const char* src = reinterpret_cast<const char*>(A.stage[C.cur] + 2 * (long long)C.off);
-  const uint32_t bytes = (uint32_t)C.n * 32u;
-  for (uint32_t o = 0; o < bytes; o += 32768u) {
-    const uint32_t b = (bytes - o < 32768u) ? bytes - o : 32768u;
-    tma_bulk_g2s(reinterpret_cast<char*>(dst) + o, src + o, b, mbar);
-  }
-}
-
-template <int G, bool ST>
-__device__ __forceinline__ void step_bead_any(const DevArrays& A, const ItemCtx& C, const float4* S,
-                                              int b, int lane, unsigned gmask) {
-  if (C.img) step_bead<G, ST, true>(A, C, S, b, lane, gmask);
-  else step_bead<G, ST>(A, C, S, b, lane, gmask);
-}
-
 // TPB: largest block size (256, or 512 for the wide variants); MB: resident
-// CTAs of TPB threads per SM the register allocation is sized for.
-//
-// Each CTA takes a contiguous block of work items and steps it in rounds.  A
-// round is as many consecutive items as fit in the CTA's shared-memory stage
-// together -- consecutive items of one replica form one segment, and every
-// segment's whole replica is staged once, all of a round's bulk copies on one
-// mbarrier phase -- and its lane groups take beads one at a time from a CTA
-// counter across all of the round's segments: a group that finishes a short
-// row goes on to the next bead of any segment, and the only barrier is the
-// one between rounds (before the stage is refilled).  Every bead's
-// arithmetic is the same whatever the rounds.
+// CTAs of TPB threads per SM the register allocation is sized for
 template <int G, int MB, int TPB = 256>
 __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* items,
                                                  const int* nitems_dev, int nitems_host) {
   const int nitems = nitems_dev ? *nitems_dev : nitems_host;
   extern __shared__ __align__(128) float4 sst[];
   __shared__ __align__(8) unsigned long long mbar;
-  __shared__ ItemCtx sC[kStepSegs];
-  __shared__ int s_b0[kStepSegs], s_pre[kStepSegs + 1], s_soff[kStepSegs];
-  __shared__ int s_nseg, s_it, s_next, s_wait;
+  __shared__ ItemCtx sC;
   const int lane = threadIdx.x & (G - 1);
+  const int grp = threadIdx.x / G, ngrp = blockDim.x / G;
   const unsigned gmask =
       (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
-  const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int it_end = min(nitems, ((int)blockIdx.x + 1) * per);
   if (threadIdx.x == 0) mbar_init(&mbar, 1);
   fence_async_smem();
   __syncthreads();
   uint32_t parity = 0;
+  // a contiguous block of items per CTA; consecutive items of one replica
+  // merge into one bead range, staged once, with no barrier inside it.  (A
+  // CTA's time is set by its chain of items, each with a fixed staging and
+  // row-latency cost, so equal item counts balance better than equal beads.)
+  const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int it_end = min(nitems, ((int)blockIdx.x + 1) * per);
   for (int it = (int)blockIdx.x * per; it < it_end;) {
+    StepItem w = items[it];
+    int nx = it + 1;
+    for (; nx < it_end; ++nx) {
+      const StepItem v = items[nx];
+      if (v.r != w.r) break;
+      w.b1 = v.b1;
+    }
+    it = nx;
     if (threadIdx.x == 0) {
-      // the round: segments while their replicas fit in the stage together
-      const int cap4 = ((int)dynamic_smem_bytes() - 128) / 16;
-      int ns = 0, off = 0, pre = 0, last_r = -1, b1 = 0;
-      while (it < it_end) {
-        const StepItem w = items[it];
-        if (w.r == last_r) {  // the next item of the segment's replica
-          b1 = w.b1;
-          it++;
-          continue;
-        }
-        if (ns == kStepSegs) break;
-        const ItemCtx C = load_ctx(A, w.r);
-        const int need = (C.phase != PH_SKIP && w.staged) ? 2 * C.n : 0;
-        if (ns > 0 && off + need > cap4) break;
-        if (ns > 0) pre += b1 - s_b0[ns - 1];
-        sC[ns] = C;
-        s_b0[ns] = w.b0;
-        s_pre[ns] = pre;
-        s_soff[ns] = need ? off : -1;
-        off += need;
-        last_r = w.r;
-        b1 = w.b1;
-        ns++;
-        it++;
-      }
-      s_pre[ns] = pre + b1 - s_b0[ns - 1];
-      s_nseg = ns;
-      s_it = it;
-      s_next = 0;
-      s_wait = off > 0;
-      if (off > 0) {
+      const ItemCtx C = load_ctx(A, w.r);
+      sC = C;
+      if (C.phase != PH_SKIP && w.staged) {
+        const char* src = reinterpret_cast<const char*>(A.stage[C.cur] + 2 * (long long)C.off);
+        const uint32_t bytes = (uint32_t)C.n * 32u;
         fence_async_smem();
-        mbar_expect_tx(&mbar, (uint32_t)off * 16u);
-        for (int k = 0; k < ns; k++)
-          if (s_soff[k] >= 0) stage_replica(A, sC[k], sst + s_soff[k], &mbar);
+        mbar_expect_tx(&mbar, bytes);
+        if (!A.skip_stage_copy)  // (diagnostics: expected but not issued)
+          for (uint32_t o = 0; o < bytes; o += 32768u) {
+            const uint32_t b = (bytes - o < 32768u) ? bytes - o : 32768u;
+            tma_bulk_g2s(reinterpret_cast<char*>(sst) + o, src + o, b, &mbar);
+          }
       }
     }
     __syncthreads();
-    it = s_it;
-    const int nseg = s_nseg, total = s_pre[nseg];
-    if (s_wait) {
-      if (!wait_staged(A, &mbar, parity)) return;
-      parity ^= 1u;
+    const ItemCtx C = sC;
+    if (C.phase != PH_SKIP) {
+      if (w.staged) {
+        const unsigned long long t0 = globaltimer_ns();
+        bool late = false;
+        while (!mbar_try_wait(&mbar, parity)) {
+          if (globaltimer_ns() - t0 > (unsigned long long)A.stage_wait_ns) {
+            late = true;
+            break;
+          }
+        }
+        if (__syncthreads_or(late)) {
+          // never expected: record it, let the copy in flight land in this
+          // CTA's shared memory (bounded), and leave the step
+          if (threadIdx.x == 0) atomicOr(A.err, 1);
+          const unsigned long long t1 = globaltimer_ns();
+          while (!mbar_try_wait(&mbar, parity) && globaltimer_ns() - t1 < kDrainNs) {
+          }
+          return;
+        }
+        parity ^= 1u;
+        if (C.img)
+          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, true, true>(A, C, sst, b, lane, gmask);
+        else
+          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, true>(A, C, sst, b, lane, gmask);
+      } else {
+        const float4* S = A.stage[C.cur] + 2 * (long long)C.off;
+        if (C.img)
+          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, false, true>(A, C, S, b, lane, gmask);
+        else
+          for (int b = w.b0 + grp; b < w.b1; b += ngrp) step_bead<G, false>(A, C, S, b, lane, gmask);
+      }
     }
-    for (;;) {
-      int g = 0;
-      if (lane == 0) g = atomicAdd(&s_next, 1);
-      g = __shfl_sync(gmask, g, 0, G);
-      if (g >= total) break;
-      int k = 0;
-      while (k + 1 < nseg && g >= s_pre[k + 1]) k++;
-      const ItemCtx& C = sC[k];
-      if (C.phase == PH_SKIP) continue;
-      const int b = s_b0[k] + (g - s_pre[k]);
-      if (s_soff[k] >= 0) step_bead_any<G, true>(A, C, sst + s_soff[k], b, lane, gmask);
-      else step_bead_any<G, false>(A, C, A.stage[C.cur] + 2 * (long long)C.off, b, lane, gmask);
-    }
-    __syncthreads();  // the round's beads are done before the stage is refilled
+    __syncthreads();
   }
 }
 
@@ -1643,6 +1607,7 @@ __device__ void step_bead64(const DevArrays& A, const ItemCtx& C, const RepDev* 
     for (int k = 0; k < nat_cnt; k++) {  // native attraction (energy.cpp:274-311)
       const int4 e = A.nat[tp.x + k];
       const int j = e.x & (int)kIdx;
+      if (!SOP_GATHER_OK(A, j, C.n)) continue;
       double dx, dy, dz;
       const double d2 = delta(j, dx, dy, dz);
       const double r0 = A.nat_r0[tp.x + k], r2 = r0 * r0;
@@ -1666,6 +1631,7 @@ __device__ void step_bead64(const DevArrays& A, const ItemCtx& C, const RepDev* 
     for (int k = 0; k < cnt; k++) {  // non-native repulsion (energy.cpp:313-350)
       const int e = A.nl[row + k];
       const int j = e & (int)kIdx;
+      if (!SOP_GATHER_OK(A, j, C.n)) continue;
       double dx, dy, dz;
       const double d2 = delta(j, dx, dy, dz);
       const int tj = (int)f2u(A.stage[C.cur][2 * ((long long)C.off + j)].w);
@@ -1686,6 +1652,7 @@ __device__ void step_bead64(const DevArrays& A, const ItemCtx& C, const RepDev* 
   if (C.terms & SOP_TERM_FENE) {
     for (int k = 0; k < bnd_cnt; k++) {  // FENE (energy.cpp:402-447)
       const int j = A.bnd[tp.y + k].x;
+      if (!SOP_GATHER_OK(A, j, C.n)) continue;
       double dx, dy, dz;
       const double d = sqrt(delta(j, dx, dy, dz));
       const double dev = d - A.bnd_r0[tp.y + k];
@@ -1698,6 +1665,7 @@ __device__ void step_bead64(const DevArrays& A, const ItemCtx& C, const RepDev* 
   if (C.terms & SOP_TERM_ANGLE) {
     for (int k = 0; k < ang_cnt; k++) {  // i,i+2 soft sphere (energy.cpp:354-400)
       const int j = A.ang[tp.z + k];
+      if (!SOP_GATHER_OK(A, j, C.n)) continue;
       double dx, dy, dz;
       const double d2 = delta(j, dx, dy, dz);
       const double d4 = d2 * d2, d8 = d4 * d4;
@@ -1821,7 +1789,7 @@ __device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b
     if (R->terms & SOP_TERM_FENE)
       for (int k = 0; k < bnd_cnt; k++) {
         const int j = A.bnd[tp.y + k].x;
-        if (j <= i) continue;
+        if (j <= i || !SOP_GATHER_OK(A, j, R->n)) continue;
         const double d = sqrt(exact_d2i(X, cap, gi, off + j, Limg));
         const double dev = d - A.bnd_r0[tp.y + k];
         eb += log1p(-dev * dev / R->R0sq_d);
@@ -1829,7 +1797,7 @@ __device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b
     if (R->terms & SOP_TERM_ANGLE)
       for (int k = 0; k < ang_cnt; k++) {
         const int j = A.ang[tp.z + k];
-        if (j <= i) continue;
+        if (j <= i || !SOP_GATHER_OK(A, j, R->n)) continue;
         const double d2 = exact_d2i(X, cap, gi, off + j, Limg);
         ea += R->e_ang_coeff / (d2 * d2 * d2);
       }
@@ -1837,7 +1805,7 @@ __device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b
       for (int k = 0; k < nat_cnt; k++) {
         const int4 e = A.nat[tp.x + k];
         const int j = e.x & (int)kIdx;
-        if (j <= i || !(e.x & (int)kPL)) continue;
+        if (j <= i || !(e.x & (int)kPL) || !SOP_GATHER_OK(A, j, R->n)) continue;
         const int tj = (int)f2u(S[2 * (off + (long long)j)].w);
         const double r0 = A.nat_r0[tp.x + k];
         const double r2 = r0 * r0, r6 = r2 * r2 * r2, r12 = r6 * r6;
@@ -1850,7 +1818,7 @@ __device__ void energy_terms(const DevArrays& A, const RepDev* R, int buf, int b
       for (int k = 0; k < cnt; k++) {
         const int e = A.nl[row + k];
         const int j = e & (int)kIdx;
-        if (j <= i || !(e & (int)kPL)) continue;
+        if (j <= i || !(e & (int)kPL) || !SOP_GATHER_OK(A, j, R->n)) continue;
         const int tj = (int)f2u(S[2 * (off + (long long)j)].w);
         const double d2 = exact_d2i(X, cap, gi, off + j, Limg);
         const double d6 = d2 * d2 * d2, d12 = d6 * d6;
@@ -1913,7 +1881,7 @@ __device__ void replica_obs(const DevArrays& A, RepDev* R, int buf, double* red)
     const int nat_cnt = tp.w & 0xFFFF;
     for (int k = 0; k < nat_cnt; k++) {
       const int j = A.nat[tp.x + k].x & (int)kIdx;
-      if (j <= i) continue;
+      if (j <= i || !SOP_GATHER_OK(A, j, n)) continue;
       const float r_ij = (float)A.nat_r0[tp.x + k];  // sop.cpp:213 reads r0 into a float
       const double d = sqrt(exact_d2i(X, cap, off + j, gi, Limg));
       q[1] += 1.0;
@@ -1998,6 +1966,7 @@ __global__ void k_pairlist(DevArrays A, int r, int off, int n) {
   for (int k = 0; k < nat_cnt; k++) {
     const int4 e = A.nat[tp.x + k];
     const int j = e.x & (int)kIdx;
+    if (!SOP_GATHER_OK(A, j, n)) continue;
     const float4 hj = S[2 * j], lj = S[2 * j + 1];
     float dx, dy, dz;
     diff(hj, lj, dx, dy, dz);
@@ -2014,6 +1983,7 @@ __global__ void k_pairlist(DevArrays A, int r, int off, int n) {
   for (int k = 0; k < cnt; k++) {
     const int e = A.nl[row + k];
     const int j = e & (int)kIdx;
+    if (!SOP_GATHER_OK(A, j, n)) continue;
     const float4 hj = S[2 * j], lj = S[2 * j + 1];
     float dx, dy, dz;
     diff(hj, lj, dx, dy, dz);

@@ -65,6 +65,11 @@ struct DevArrays {
   float group_frac2;  // (grouping fraction of the trigger distance)^2; > 1 = no grouping
 };
 
+// Bits of the engine's error word (DevArrays::err): 1 and 2 a bounded wait
+// ran out (staging copy, work queue); kErrIndex a checked build found a
+// partner index outside its replica.
+constexpr int kErrIndex = 4;
+
 // Grid of one replica's last binning.
 struct BinHdr {
   int ok, status, nx, ny, nz, K, ncell;  // K: stencil half-width in cells

@@ -12,15 +12,19 @@ from concurrent.futures import ThreadPoolExecutor
 import numpy as np
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIB_PATH = os.path.join(PKG_DIR, "lib", "libsopgpu.so")
+# SOP_GB300_CHECKED=1 selects the checked build (every partner index tested
+# against its replica's range; a bad one fails the call with SOP_ERR_INDEX)
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libsopgpu_checked.so"
+                        if os.environ.get("SOP_GB300_CHECKED") == "1" else "libsopgpu.so")
 
 SOP_OK = 0
 ERRORS = {
     -1: "SOP_ERR_ARG", -2: "SOP_ERR_CUDA", -3: "SOP_ERR_NOMEM", -4: "SOP_ERR_STATE",
     -5: "SOP_ERR_OVERFLOW", -6: "SOP_ERR_UNSUPPORTED", -7: "SOP_ERR_NODEV",
-    -8: "SOP_ERR_REPLICA", -9: "SOP_ERR_FULL", -10: "SOP_ERR_TIMEOUT",
+    -8: "SOP_ERR_REPLICA", -9: "SOP_ERR_FULL", -10: "SOP_ERR_TIMEOUT", -11: "SOP_ERR_INDEX",
 }
 ERR_TIMEOUT = -10
+ERR_INDEX = -11
 ST_NONFINITE, ST_FENE, ST_LIST_OVERFLOW, ST_PERIODIC, ST_GRID = 1, 2, 4, 8, 16
 LIST_NONE, LIST_NEIGHBOR, LIST_CELL, LIST_SKIN = 0, 1, 2, 3
 TERM_RANDOM, TERM_FENE, TERM_ANGLE, TERM_VDW, TERM_ALL = 1, 2, 4, 8, 15

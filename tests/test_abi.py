@@ -24,8 +24,9 @@ def test_header_and_binding_agree():
     assert declared_functions() == sorted(L.exported_symbols())
 
 
-def test_library_exports_every_declared_symbol():
-    lib = C.CDLL(L.LIB_PATH)
+@pytest.mark.parametrize("name", ["libsopgpu.so", "libsopgpu_checked.so"])
+def test_library_exports_every_declared_symbol(name):
+    lib = C.CDLL(os.path.join(os.path.dirname(L.LIB_PATH), name))
     missing = [f for f in declared_functions() if not hasattr(lib, f)]
     assert not missing
 
