@@ -164,6 +164,12 @@ typedef struct sop_engine_config {
    * calls work (restore or re-add the replicas that call stepped). */
   int64_t queue_wait_ns;
   int64_t stage_wait_ns;
+  /* How the batched step's work items (sorted by replica size, largest
+   * first) are split into one contiguous block per CTA: <0 = equal item
+   * counts; >= 0 = equal estimated cost, an item costing its beads plus this
+   * many bead equivalents for the fixed per-item work (0 = 512).  Same
+   * results either way. */
+  int item_cost_beads;
 } sop_engine_config;
 
 /* ---- engine -------------------------------------------------------------- */

@@ -90,6 +90,9 @@ struct sop_engine {
   bool has64 = false;                  // an FP64 replica was ever laid out (k_step64 launched)
   int max_n = 0, max_staged = 0, step_grid = 1, pro_grid = 1;
   int* d_counts = nullptr;          // {active replicas, work items}, read by the kernels
+  int* d_cta_first = nullptr;       // per step CTA, its first work item (cost-balanced split)
+  int cta_first_cap = 0;
+  std::vector<int> h_cta_first;
   // packed host-order state of sop_run_host (one copy each way)
   double* d_pack_xyz = nullptr;
   double* d_pack_vel = nullptr;
@@ -132,6 +135,7 @@ struct LaunchShape {
   int strategy;    // 0 CTA items, 1 warp tasks
   int lanes;       // lanes per bead
   int group_pct;   // grouped skin rebuilds (0 = off)
+  int item_cost;   // step CTA blocks by estimated cost (bead equivalents per item; <0 = equal counts)
 };
 LaunchShape get_launch_shape(const sop_engine* e);
 // recompute the persistent grid, invalidate layout and graph

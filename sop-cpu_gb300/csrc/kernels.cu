@@ -1437,7 +1437,8 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
 // CTAs of TPB threads per SM the register allocation is sized for
 template <int G, int MB, int TPB = 256>
 __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* items,
-                                                 const int* nitems_dev, int nitems_host) {
+                                                 const int* nitems_dev, int nitems_host,
+                                                 const int* cta_first) {
   const int nitems = nitems_dev ? *nitems_dev : nitems_host;
   extern __shared__ __align__(128) float4 sst[];
   __shared__ __align__(8) unsigned long long mbar;
@@ -1450,13 +1451,16 @@ __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* i
   fence_async_smem();
   __syncthreads();
   uint32_t parity = 0;
-  // a contiguous block of items per CTA; consecutive items of one replica
-  // merge into one bead range, staged once, with no barrier inside it.  (A
-  // CTA's time is set by its chain of items, each with a fixed staging and
-  // row-latency cost, so equal item counts balance better than equal beads.)
+  // a contiguous block of items per CTA: [cta_first[b], cta_first[b + 1])
+  // when the host split the items by estimated cost, else equal item counts;
+  // consecutive items of one replica merge into one bead range, staged once,
+  // with no barrier inside it.  (A CTA's time is set by its chain of items,
+  // each with a fixed staging and row-latency cost on top of its beads.)
   const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int it_end = min(nitems, ((int)blockIdx.x + 1) * per);
-  for (int it = (int)blockIdx.x * per; it < it_end;) {
+  const int it0 = cta_first ? min(nitems, cta_first[blockIdx.x]) : (int)blockIdx.x * per;
+  const int it_end = cta_first ? min(nitems, cta_first[blockIdx.x + 1])
+                               : min(nitems, ((int)blockIdx.x + 1) * per);
+  for (int it = it0; it < it_end;) {
     StepItem w = items[it];
     int nx = it + 1;
     for (; nx < it_end; ++nx) {
@@ -1526,7 +1530,8 @@ __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* i
 // finished warps; the last warp resets both for the next launch.
 template <int G, int MB>
 __global__ void __launch_bounds__(256, MB) k_step_w(DevArrays A, const StepItem* items,
-                                                   const int* nitems_dev, int nitems_host) {
+                                                   const int* nitems_dev, int nitems_host,
+                                                   const int*) {
   const int nitems = nitems_dev ? *nitems_dev : nitems_host;
   const int l32 = threadIdx.x & 31;
   const int lane = l32 & (G - 1), grp = l32 / G;
@@ -2084,7 +2089,7 @@ __global__ void k_export(DevArrays A, int r, int off, int n, int which, int capa
 // ---------------------------------------------------------------------------------
 // launchers
 
-using StepKernel = void (*)(DevArrays, const StepItem*, const int*, int);
+using StepKernel = void (*)(DevArrays, const StepItem*, const int*, int, const int*);
 
 // The step kernel for a strategy (0: CTA items with shared-memory staging,
 // 1: warp tasks), lane count (1, 2, 4, 8, 16) and occupancy target (2, 3,
@@ -2180,14 +2185,14 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, co
 }
 
 cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
-                        int max_staged, int lanes, int min_blocks, int strategy, int threads,
-                        int grid, cudaStream_t s) {
+                        const int* cta_first, int max_staged, int lanes, int min_blocks,
+                        int strategy, int threads, int grid, cudaStream_t s) {
   if (nitems <= 0) return cudaSuccess;
   const size_t dyn = strategy == 1 ? 0 : (size_t)max_staged * 32 + 128;
   if (grid <= 0) grid = nitems;
   if (!step_shape_supported(lanes, strategy, threads)) return cudaErrorInvalidConfiguration;
   step_kernel(lanes, min_blocks, strategy, threads)<<<grid, threads, dyn, s>>>(A, items, nitems_dev,
-                                                                              nitems);
+                                                                              nitems, cta_first);
   return cudaGetLastError();
 }
 

@@ -123,9 +123,11 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, co
 // resident CTAs per SM
 // strategy: 0 = CTA work items with shared-memory staging (k_step), 1 = warp
 // tasks gathering through L1/L2 (k_step_w); bit-identical results
+// cta_first: grid + 1 item boundaries, CTA b steps items [cta_first[b],
+// cta_first[b + 1]) (the CTA strategy; null = equal item counts)
 cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
-                        int max_staged, int lanes, int min_blocks, int strategy, int threads,
-                        int grid, cudaStream_t s);
+                        const int* cta_first, int max_staged, int lanes, int min_blocks,
+                        int strategy, int threads, int grid, cudaStream_t s);
 // the FP64-precision step over its own items (one thread per bead)
 cudaError_t launch_step64(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
                           int grid, cudaStream_t s);

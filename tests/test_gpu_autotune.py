@@ -81,6 +81,7 @@ def test_list_tuning_keeps_reference_pair_sets():
 @pytest.mark.parametrize("cfg", [dict(step_strategy=1), dict(step_strategy=1, step_min_blocks=2),
                                  dict(step_min_blocks=3, stage_limit=2048), dict(step_min_blocks=2),
                                  dict(stage_limit=-1), dict(build_slice_beads=128, chunk_beads=64),
+                                 dict(item_cost_beads=-1), dict(item_cost_beads=16, chunk_beads=64),
                                  dict(lanes_per_bead=4), dict(lanes_per_bead=1), dict(block_threads=64),
                                  dict(block_threads=128, lanes_per_bead=4, chunk_beads=512),
                                  dict(group_rebuild_pct=-1), dict(group_rebuild_pct=90),
