@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-steps", default="100,10000", help="log-uniform step-count range")
     ap.add_argument("--serve-chunk", type=int, default=100)
+    ap.add_argument("--serve-active", type=int, default=2048,
+                    help="most requests the server keeps resident (stepped together)")
     ap.add_argument("--large-chains", type=int, default=100,
                     help="single large system: chains x --large-len beads (0 = skip)")
     ap.add_argument("--large-len", type=int, default=500)
@@ -395,7 +397,7 @@ def serve_stream(args, rank):
     params = [make_params(workload_script(), T=float(temps[k]), seed=90_000 + k,
                           list_mode=args.list_mode, skin=args.skin, pull_force=float(pulls[k]))
               for k in range(nreq)]
-    srv = Server(0, max_active=2048, chunk_steps=args.serve_chunk, max_beads=1 << 21,
+    srv = Server(0, max_active=args.serve_active, chunk_steps=args.serve_chunk, max_beads=1 << 21,
                  max_replicas=2100, max_list_entries=(1 << 21) * 96)
     # warm-up requests, not timed
     for k in range(8):
@@ -434,7 +436,8 @@ def serve_stream(args, rank):
                       "seeded chains), steps log-uniform %g-%g%s, T 0.4-0.9, pull 0-15 pN"
                       % (args.serve_rate, args.serve_seconds, len(pool), lo, hi,
                          "" if (lo, hi) == (1e4, 1e6) else
-                         " (the serving configuration's 1e4-1e6 scaled)")}
+                         " (the serving configuration's 1e4-1e6 scaled)"),
+            "max_active": args.serve_active}
 
 
 def force_err(eng, r, s):
@@ -477,9 +480,11 @@ def force_check(eng, ids, systems, count=4):
 def single_system(args):
     """One compact chain of --single-len beads (3000, seed 1000) on its own: the
     plain single-system path (one replica, the reference's neighbor-list
-    cadence, nnlup 10, underdamped, T 0.6, noise on), --single-steps steps in
-    windows of 1000; after each window the force at the current state against
-    the CPU oracle (FP64 reference formulas), as the check every 1000 steps."""
+    cadence, nnlup 10, underdamped, T 0.6, noise on), the launch shape tuned for
+    it during warm-up (--autotune steps per trial; trials are real steps),
+    --single-steps steps in windows of 1000; after each window the force at the
+    current state against the CPU oracle (FP64 reference formulas), as the
+    check every 1000 steps."""
     from sop_gb300 import systems as S
     from sop_gb300.engine import Engine, make_params
     s = S.synth_chain(1000, args.single_len)
@@ -488,6 +493,10 @@ def single_system(args):
     with Engine(0, max_beads=max(1 << 14, 2 * n), max_replicas=4, max_list_entries=n * 400) as eng:
         r = eng.add(s, make_params(workload_script(), seed=1000))
         eng.run(50)  # warm
+        tuned = None
+        if args.autotune > 0:  # launch shape for one replica (its trials are real steps)
+            report = eng.autotune(args.autotune, shape=True, lists=False)
+            tuned = [l for l in report.splitlines() if l.startswith("chosen")]
         total, errs = 0.0, []
         for _ in range(windows):
             eng.run(1000)
@@ -496,7 +505,8 @@ def single_system(args):
         status = eng.status(r)[0]
     return {"workload": "one compact chain of %d beads, neighbor-list cadence (nnlup 10), T 0.6" % n,
             "steps": 1000 * windows, "bead_steps_per_s": n * 1000 * windows / (total / 1e3),
-            "force_rel_err_max": max(errs), "force_checks": len(errs), "status": status}
+            "force_rel_err_max": max(errs), "force_checks": len(errs), "status": status,
+            "autotuned": tuned}
 
 
 def measure_l2_gbs(device):

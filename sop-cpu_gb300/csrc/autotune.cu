@@ -128,9 +128,9 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
   const std::vector<Knob> knobs = {
       {"warp", &LaunchShape::strategy, {0, 1}},
       {"stage", &LaunchShape::stage, stages},
-      {"chunk", &LaunchShape::chunk, {64, 128, 256, 512}},
+      {"chunk", &LaunchShape::chunk, {32, 64, 128, 256, 512}},
       {"threads", &LaunchShape::threads, {64, 128, 256, 512}},
-      {"lanes", &LaunchShape::lanes, {1, 2, 4}},
+      {"lanes", &LaunchShape::lanes, {1, 2, 4, 8, 16}},
       {"occ", &LaunchShape::min_blocks, {2, 3, 4}},
       {"slice", &LaunchShape::slice, {16, 32, 64, 128}},
       {"group", &LaunchShape::group_pct, {0, 30, 50, 70}},
