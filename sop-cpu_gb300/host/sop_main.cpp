@@ -178,11 +178,30 @@ std::vector<std::string> split(const std::string& s) {
   return out;
 }
 
+// A data file is refused, with the reason on stderr, when it declares more
+// entries than it holds, when an entry has too few fields, or when a bead
+// index is not 1..kMaxBeads (the reference reads such files without checks,
+// params.cpp:110-260; indices past the loaded chain are refused by the engine).
+constexpr long long kMaxBeads = 1LL << 22;
+
+bool bad_entry(const std::string& file, long long k, const char* why) {
+  std::fprintf(stderr, "%s: entry %lld: %s\n", file.c_str(), k + 1, why);
+  return false;
+}
+
+bool bead_index(const std::string& tok, int* out) {
+  const long long v = std::atoll(tok.c_str());
+  if (v < 1 || v > kMaxBeads) return false;
+  *out = (int)(v - 1);
+  return true;
+}
+
 bool load(const Command& c, Topology& top) {
   if (c.opt.size() < 2) return false;
-  std::ifstream in(c.opt[1]);
+  const std::string& file = c.opt[1];
+  std::ifstream in(file);
   if (!in) {
-    std::fprintf(stderr, "cannot open %s\n", c.opt[1].c_str());
+    std::fprintf(stderr, "cannot open %s\n", file.c_str());
     return false;
   }
   std::string line;
@@ -190,29 +209,38 @@ bool load(const Command& c, Topology& top) {
   const std::vector<std::string> head = split(line);
   const std::string& what = c.opt[0];
   if (what == "bonds" && head.size() >= 2) {  // params.cpp:126-144
-    const int n = std::atoi(head[1].c_str());
-    for (int k = 0; k < n && std::getline(in, line); k++) {
+    const long long n = std::atoll(head[1].c_str());
+    for (long long k = 0; k < n; k++) {
+      if (!std::getline(in, line)) return bad_entry(file, k, "missing (the header declares more)");
       const auto t = split(line);
-      if (t.size() < 3) return false;
-      top.ib.push_back(std::atoi(t[0].c_str()) - 1);
-      top.jb.push_back(std::atoi(t[1].c_str()) - 1);
+      int i, j;
+      if (t.size() < 3) return bad_entry(file, k, "fewer than 3 fields");
+      if (!bead_index(t[0], &i) || !bead_index(t[1], &j)) return bad_entry(file, k, "bead index out of range");
+      top.ib.push_back(i);
+      top.jb.push_back(j);
       top.r0.push_back(std::atof(t[2].c_str()));
     }
   } else if (what == "angles" && head.size() >= 2) {  // params.cpp:145-165
-    const int n = std::atoi(head[1].c_str());
-    for (int k = 0; k < n && std::getline(in, line); k++) {
+    const long long n = std::atoll(head[1].c_str());
+    for (long long k = 0; k < n; k++) {
+      if (!std::getline(in, line)) return bad_entry(file, k, "missing (the header declares more)");
       const auto t = split(line);
-      if (t.size() < 4) return false;
-      top.ia.push_back(std::atoi(t[0].c_str()) - 1);
-      top.ka.push_back(std::atoi(t[2].c_str()) - 1);
+      int i, j, m;
+      if (t.size() < 4) return bad_entry(file, k, "fewer than 4 fields");
+      if (!bead_index(t[0], &i) || !bead_index(t[1], &j) || !bead_index(t[2], &m))
+        return bad_entry(file, k, "bead index out of range");
+      top.ia.push_back(i);
+      top.ka.push_back(m);
     }
   } else if (what == "vdw" && head.size() >= 4) {  // params.cpp:166-234
     const long long n = std::atoll(head[1].c_str()) + std::atoll(head[3].c_str());
     top.have_vdw = true;
-    for (long long k = 0; k < n && std::getline(in, line); k++) {
+    for (long long k = 0; k < n; k++) {
+      if (!std::getline(in, line)) return bad_entry(file, k, "missing (the header declares more)");
       const auto t = split(line);
-      if (t.size() < 5) return false;
-      const int i = std::atoi(t[0].c_str()) - 1, j = std::atoi(t[1].c_str()) - 1;
+      int i, j;
+      if (t.size() < 5) return bad_entry(file, k, "fewer than 5 fields");
+      if (!bead_index(t[0], &i) || !bead_index(t[1], &j)) return bad_entry(file, k, "bead index out of range");
       const double r = std::atof(t[2].c_str());
       const int ti = std::atoi(t[3].c_str()), tj = std::atoi(t[4].c_str());
       if ((int)top.type.size() < std::max(i, j) + 1) top.type.resize(std::max(i, j) + 1, 1);
@@ -226,14 +254,21 @@ bool load(const Command& c, Topology& top) {
       top.rep_pairs.push_back({std::min(i, j), std::max(i, j)});
     }
   } else if (what == "init" && head.size() >= 2) {  // params.cpp:235-258
-    top.nbead = std::atoi(head[1].c_str());
+    const long long n = std::atoll(head[1].c_str());
+    if (n < 1 || n > kMaxBeads) {
+      std::fprintf(stderr, "%s: bead count %lld out of range\n", file.c_str(), n);
+      return false;
+    }
+    top.nbead = (int)n;
     top.xyz.assign(3 * (size_t)top.nbead, 0.0);
-    for (int k = 0; k < top.nbead && std::getline(in, line); k++) {
+    for (long long k = 0; k < n; k++) {
+      if (!std::getline(in, line)) return bad_entry(file, k, "missing (the header declares more)");
       const auto t = split(line);
-      if (t.size() < 4) return false;
+      if (t.size() < 4) return bad_entry(file, k, "fewer than 4 fields");
       for (int q = 0; q < 3; q++) top.xyz[3 * k + q] = std::atof(t[1 + q].c_str());
     }
   } else {
+    std::fprintf(stderr, "%s: unknown data kind '%s' or header\n", file.c_str(), what.c_str());
     return false;
   }
   return true;
@@ -272,11 +307,14 @@ void append_frame(const std::string& fname, const std::vector<double>& x, int n)
   std::fclose(f);
 }
 
+// n coordinate lines "index x y z" (io.cpp's coordinate format); false when
+// the file is missing or holds fewer.
 bool read_coords(const std::string& fname, std::vector<double>& x, int n) {
   std::ifstream in(fname);
   if (!in) return false;
   std::string line;
-  for (int i = 0; i < n && std::getline(in, line); i++) {
+  for (int i = 0; i < n; i++) {
+    if (!std::getline(in, line)) return false;
     const auto t = split(line);
     if (t.size() < 4) return false;
     for (int q = 0; q < 3; q++) x[3 * i + q] = std::atof(t[1 + q].c_str());
@@ -357,8 +395,13 @@ int main(int argc, char** argv) {
       }
       double istep = 1.0;
       if (S.restart) {  // sop.cpp:132-136: coordinates and velocities from files
-        if (read_coords(S.unccfname, unc, n) && read_coords(S.vfname, vel, n))
-          check(sop_replica_set_state(eng, rep, unc.data(), vel.data()), "sop_replica_set_state");
+        for (const std::string* f : {&S.unccfname, &S.vfname}) {
+          if (!read_coords(*f, f == &S.vfname ? vel : unc, n)) {
+            std::fprintf(stderr, "restart: cannot read %d beads from %s\n", n, f->c_str());
+            return 1;
+          }
+        }
+        check(sop_replica_set_state(eng, rep, unc.data(), vel.data()), "sop_replica_set_state");
         istep = S.istep_restart + 1.0;
         if (S.rgen_restart) check(sop_replica_set_step(eng, rep, (int64_t)S.istep_restart), "set_step");
       }
