@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--list-mode", default="skin", choices=["neighborlist", "skin"])
     ap.add_argument("--skin", type=float, default=3.0)
     ap.add_argument("--plain-steps", type=int, default=20)
+    ap.add_argument("--full-steps", type=int, default=200000,
+                    help="MD steps of every replica in one run after the timed region (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
@@ -576,6 +578,17 @@ def run_gb300(args):
     achieved = algo / (step_ms / 1e3) / 1e9
     l2_gbs = measure_l2_gbs(local)
 
+    # the batched configuration's whole horizon (--full-steps MD steps of every
+    # replica, grouped rebuilds included) in one run call
+    full = None
+    if args.full_steps > 0:
+        eng.run(args.full_steps)
+        full_ms = eng.timing()[0]
+        bad = sum(1 for r in ids if eng.status(r)[0])
+        full = {"md_steps": args.full_steps, "bead_steps": beads * args.full_steps,
+                "bead_steps_per_s": beads * args.full_steps / (full_ms / 1e3), "wall_s": full_ms / 1e3,
+                "replicas_with_error_status": bad}
+
     # end to end through the host-buffer C call
     nb3 = 3 * beads
     xin = torch.empty(nb3, dtype=torch.float64, pin_memory=True).numpy()
@@ -628,6 +641,7 @@ def run_gb300(args):
         "gpu_launches": int(launches),
         "plain_gpu_path": {"value": plain, "unit": UNIT, "steps": args.plain_steps,
                            "batched_over_plain": value / plain},
+        "full_horizon": full,
         "served": served,
         "large_system": large,
         "single_system": single,
