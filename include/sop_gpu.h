@@ -170,6 +170,12 @@ typedef struct sop_engine_config {
    * many bead equivalents for the fixed per-item work (0 = 512).  Same
    * results either way. */
   int item_cost_beads;
+  /* Far entries of the list rows (farther than the pair cutoff plus a band
+   * width -- half the skin, or 0.35 sigma for cadence lists -- at the
+   * build) are stored last, and the step skips them while no bead of the
+   * replica has moved half the band width since the build: they cannot be
+   * in the pair list then.  0 = on, <0 = off (same results either way). */
+  int row_bands;
 } sop_engine_config;
 
 /* ---- engine -------------------------------------------------------------- */

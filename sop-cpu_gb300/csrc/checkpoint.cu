@@ -179,6 +179,9 @@ extern "C" int sop_replica_restore(sop_engine* e, int r, const void* buf, int64_
   d.t = s.t; d.t_end = s.t_end; d.t_cur = s.t_cur; d.phase = s.phase;
   d.first_pending = s.first_pending; d.moved = s.moved; d.cur = s.cur; d.inlup = s.inlup;
   d.rebuild = s.rebuild; d.near = s.near; d.out = s.out; d.obs_pending = s.obs_pending;
+  // the snapshot's rows carry no near / far split: scan them whole until the
+  // next build (same results, the far entries' pair-list bits are 0)
+  d.wide = 1;
   d.en_after = s.en_after; d.running = s.running; d.status = s.status; d.max_row = s.max_row;
   d.builds = s.builds;
   std::memcpy(d.energy, s.energy, sizeof d.energy);

@@ -237,6 +237,7 @@ static int engine_init(sop_engine* e) {
   CK(dalloc(&A.topo, cap));
   CK(dalloc(&A.exc_rng, cap));
   CK(dalloc(&A.nl_cnt, cap));
+  CK(dalloc(&A.nl_near, cap));
   CK(dalloc(&A.nl, lcap));
   CK(dalloc(&A.nat, ecap));
   CK(dalloc(&A.nat_r0, ecap));
@@ -261,6 +262,7 @@ static int engine_init(sop_engine* e) {
                       : 4.0f;
   CK(cudaMemsetAsync(A.err, 0, sizeof(int), e->stream));
   A.queue_wait_ns = cfg.queue_wait_ns;
+  A.row_bands = cfg.row_bands >= 0 ? 1 : 0;
   A.stage_wait_ns = cfg.stage_wait_ns;
   A.publish_delay_ns = 0;
   A.skip_stage_copy = 0;
@@ -361,6 +363,7 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
     cfg.lean_prep = cfg_in->lean_prep < 0 ? -1 : 0;
     if (cfg_in->queue_wait_ns > 0) cfg.queue_wait_ns = std::min<int64_t>(cfg_in->queue_wait_ns, kMaxWaitNs);
     if (cfg_in->stage_wait_ns > 0) cfg.stage_wait_ns = std::min<int64_t>(cfg_in->stage_wait_ns, kMaxWaitNs);
+    cfg.row_bands = cfg_in->row_bands < 0 ? -1 : 0;
     if (cfg_in->item_cost_beads != 0) cfg.item_cost_beads = std::min(cfg_in->item_cost_beads, 1 << 20);
   }
   if (cfg.group_rebuild_pct < 0 || cfg.group_rebuild_pct >= 100) cfg.group_rebuild_pct = 0;
@@ -400,7 +403,7 @@ extern "C" int sop_engine_destroy(sop_engine* e) {
   if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
   DevArrays& A = e->A;
   void* ptrs[] = {A.X[0], A.X[1], A.stage[0], A.stage[1], A.incr, A.incr64, A.vel, A.force, A.xb, A.topo,
-                  A.exc_rng, A.nl_cnt, A.nl, A.nat, A.nat_r0, A.bnd, A.bnd_r0, A.ang, A.exc,
+                  A.exc_rng, A.nl_cnt, A.nl_near, A.nl, A.nat, A.nat_r0, A.bnd, A.bnd_r0, A.ang, A.exc,
                   A.rep, A.pairs_out, A.pairs_cnt, A.err, A.units, A.unit_cnt, A.slice_done,
                   A.done_list, A.done_cnt, e->d_ids, e->d_items, e->d_items64, e->d_counts, e->d_cta_first,
                   e->d_pack_xyz,
@@ -945,6 +948,7 @@ static int place(sop_engine* e, const sop_prepared& P, int* replica) {
   CK(h2d(e->A.ang + ab, T.ang.data(), T.ang.size(), e->stream));
   CK(h2d(e->A.exc + xb, T.exc.data(), T.exc.size(), e->stream));
   CK(cudaMemsetAsync(e->A.nl_cnt + off, 0, sizeof(int) * n, e->stream));
+  CK(cudaMemsetAsync(e->A.nl_near + off, 0, sizeof(int) * n, e->stream));
   RepDev rd;
   std::memset(&rd, 0, sizeof rd);
   fill_repdev(P.params, rd);
@@ -964,6 +968,7 @@ static int place(sop_engine* e, const sop_prepared& P, int* replica) {
   rd.cur = 0;
   rd.inlup = 1;
   rd.active = 1;
+  rd.wide = 1;  // no band split of the rows until their first build
   CK(cudaMemcpyAsync(e->A.rep + slot, &rd, sizeof rd, cudaMemcpyHostToDevice, e->stream));
   int rc = stage_state(e, slot, P.xyz.data(), P.vel.empty() ? nullptr : P.vel.data());
   if (rc) return rc;

@@ -381,7 +381,16 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
       h.ncell = h.nx * h.ny * h.nz;
       h.ok = !(h.status & SOP_ST_GRID);
     }
-    // the replica's cutoffs, once per binning instead of once per listed bead
+    // the replica's cutoffs, once per binning instead of once per listed bead.
+    // Band width w: half the skin (skin lists), else 0.35 of the smallest
+    // sigma present (half the 3.2 - 2.5 sigma gap of neighbor lists; any w
+    // is exact, it only sets how many entries are far)
+    double sig_min = 1e30;
+    const int tm = R->type_mask ? R->type_mask : 0x6;
+    for (int a = 1; a < kMaxTypes; a++)
+      for (int b = 1; b < kMaxTypes; b++)
+        if (((tm >> a) & 1) && ((tm >> b) & 1)) sig_min = fmin(sig_min, c_ff.sigma_rep[a][b]);
+    const double band_w = (mode == SOP_LIST_SKIN) ? 0.5 * (double)R->skin : 0.35 * sig_min;
     for (int a = 0; a < kMaxTypes; a++)
       for (int b = 0; b < 2; b++) {
         const int ta = a ? a : 1, tb = b + 1;
@@ -390,7 +399,11 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
         h.pl2d[a][b] = c_ff.rc2_pl[ta][tb];  // (2.5 sigma)^2, sop.cpp:539-541
         h.rl2f[a][b] = (float)h.rl2d[a][b];
         h.pl2f[a][b] = (float)h.pl2d[a][b];
+        const double bd = 2.5 * c_ff.sigma_rep[ta][tb] + band_w;
+        h.bandf[a][b] = A.row_bands ? (float)(bd * bd) : 3.0e38f;  // off: nothing is far
       }
+    const double half_w = fmax(0.5 * band_w - 0.01, 0.0);
+    R->wide2 = (float)(half_w * half_w);
     H = h;
   }
   __syncthreads();
@@ -700,23 +713,60 @@ __device__ void build_slice(const DevArrays& A, int r, int src, int mode, int b0
       cnt += __popc(m);
       cntp += __popc(mp);
     }
-    if (cnt <= L && cnt > cntp) {
-      // move the back block [L - (cnt - cntp), L) down to cntp (dest <= src,
-      // 32 entries at a time, each chunk read before it is written)
+    int near_end = min(cnt, L);  // row entries [near_end, cnt) are far
+    const int nsk = cnt - cntp;
+    if (cnt <= L && nsk > 0) {
+      const long long src = row + L - nsk, dst = row + cntp;
       __syncwarp();
-      const long long src = row + L - (cnt - cntp), dst = row + cntp;
-      for (int k0 = 0; k0 < cnt - cntp; k0 += 32) {
-        const int k = k0 + lane;
-        const int v = k < cnt - cntp ? A.nl[src + k] : 0;
-        __syncwarp();
-        if (k < cnt - cntp) A.nl[dst + k] = v;
-        __syncwarp();
+      if (mode != SOP_LIST_NONE && cnt + nsk <= L) {
+        // the skin block [L - nsk, L) does not overlap [cntp, cnt): copy its
+        // near entries down first, then its far ones (farther than the pair
+        // cutoff plus the band width at these positions, with the screen's
+        // relative band as a margin: an entry in doubt counts as near)
+        int w0 = cntp;
+        for (int pass = 0; pass < 2; pass++) {
+          if (pass == 1) near_end = w0;
+          for (int k0 = 0; k0 < nsk; k0 += 32) {
+            const int k = k0 + lane;
+            bool take = false;
+            int v = 0;
+            if (k < nsk) {
+              v = A.nl[src + k];
+              const int j = v & (int)kIdx;
+              const float4 pj = P[j];
+              float ddx = pj.x - pi.x, ddy = pj.y - pi.y, ddz = pj.z - pi.z;
+              if (img) {
+                ddx = image_f(ddx, Lf, invLf);
+                ddy = image_f(ddy, Lf, invLf);
+                ddz = image_f(ddz, Lf, invLf);
+              }
+              const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+              const int tj = __float_as_int(pj.w) & 3;
+              const bool far = d2 > H->bandf[ti][tj == 2] * (1.0f + margin);
+              take = pass == 0 ? !far : far;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, take);
+            if (take) A.nl[dst - cntp + w0 + __popc(m & lt_mask)] = v;
+            w0 += __popc(m);
+          }
+        }
+      } else {
+        // move the back block down to cntp (dest <= src, 32 entries at a
+        // time, each chunk read before it is written); no far part
+        for (int k0 = 0; k0 < nsk; k0 += 32) {
+          const int k = k0 + lane;
+          const int v = k < nsk ? A.nl[src + k] : 0;
+          __syncwarp();
+          if (k < nsk) A.nl[dst + k] = v;
+          __syncwarp();
+        }
       }
     }
     if (lane == 0) {
       if (cnt > L) my_status |= SOP_ST_LIST_OVERFLOW;
       my_max = max(my_max, cnt);
       A.nl_cnt[off + i] = min(cnt, L);
+      A.nl_near[off + i] = near_end;
       const float4 h = S[2 * i];
       A.xb[off + i] = make_float4(h.x, h.y, h.z, 0.f);
     }
@@ -919,6 +969,7 @@ __device__ void run_unit(const DevArrays& A, int4 w, BuildSmem& B, unsigned char
         R->builds += 1;
         R->rebuild = 0;
         R->near = 0;
+        R->wide = 0;
       }
       if (R->en_after) replica_energy(A, R, R->cur, red);
     }
@@ -1080,6 +1131,9 @@ struct ItemCtx {
   int pull_i, pull_j;
   unsigned seed_lo, seed_hi;
   int img;        // minimum images apply (the box itself is read per bead)
+  int far_skip;   // no bead moved half the band width since the build: rows'
+                  // far entries cannot be in the pair list and are not scanned
+  float wide2;    // squared displacement past which that stops (RepDev::wide2)
 };
 
 // The box of an image-mode replica: FP32 two-float for the staged
@@ -1110,6 +1164,8 @@ __device__ __forceinline__ ItemCtx load_ctx(const DevArrays& A, int r) {
   C.amp = R->noise_amp; C.T = R->T; C.kbnd = R->kbnd; C.inv_R0sq = R->inv_R0sq; C.fang = R->fang;
   C.half_skin2 = R->half_skin2; C.pull_f = R->pull_f; C.pull_i = R->pull_i;
   C.img = R->img;
+  C.far_skip = R->mode != SOP_LIST_NONE && !R->wide;
+  C.wide2 = R->wide2;
   C.pull_j = R->pull_j; C.seed_lo = R->seed_lo; C.seed_hi = R->seed_hi;
   // a list build of this step that failed (row overflow, grid, periodic
   // image) leaves the replica frozen: no step on incomplete lists
@@ -1342,15 +1398,23 @@ __device__ __forceinline__ void bead_tail(const DevArrays& A, const ItemCtx& C, 
       }
       A.stage[nb][2 * g] = make_float4(h[0], h[1], h[2], b.hi.w);
       A.stage[nb][2 * g + 1] = make_float4(l[0], l[1], l[2], b.lo.w);
-      if (C.mode == SOP_LIST_SKIN) {
+      if (C.mode != SOP_LIST_NONE) {  // displacement since the last list build
         const float4 xb = A.xb[g];
         const float ex = h[0] - xb.x, ey = h[1] - xb.y, ez = h[2] - xb.z;
         const float d2 = ex * ex + ey * ey + ez * ez;
-        if (d2 > C.half_skin2) {
-          A.rep[C.r].rebuild = 1;
-          *A.any_rebuild = 1;
-        } else if (d2 > C.half_skin2 * A.group_frac2) {
-          A.rep[C.r].near = 1;  // may rebuild with the next replica that must
+        // (h and xb are rounded to float: a displacement within 2 ulps of the
+        // limit, or coordinates so large that 2 ulps exceed the 0.01 A slack
+        // in wide2, count as past it)
+        const float ulp2 = 2.4e-7f * fmaxf(fabsf(h[0]), fmaxf(fabsf(h[1]), fabsf(h[2])));
+        if (C.far_skip && (d2 > C.wide2 || ulp2 > 0.005f))
+          A.rep[C.r].wide = 1;  // far entries are scanned from the next step
+        if (C.mode == SOP_LIST_SKIN) {
+          if (d2 > C.half_skin2) {
+            A.rep[C.r].rebuild = 1;
+            *A.any_rebuild = 1;
+          } else if (d2 > C.half_skin2 * A.group_frac2) {
+            A.rep[C.r].near = 1;  // may rebuild with the next replica that must
+          }
         }
       }
       if (!(isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]))) st |= SOP_ST_NONFINITE;
@@ -1372,8 +1436,12 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   const int4 tp = A.topo[b.g];
   // the non-native row: rows start 32-byte aligned and hold a multiple of 8
   // entries, so a lane reads four entries with one 16-byte load (never past
-  // the row); the lane's first quad is in flight during the natives
-  const int cnt = A.nl_cnt[b.g];
+  // the row); the lane's first quad is in flight during the natives.  While
+  // no bead of the replica has moved half the band width since the build,
+  // the row's far entries (farther than the pair cutoff plus the band width
+  // at the build) cannot be in the pair list: their bits stay 0 and they are
+  // not scanned (the pair filter stays exact)
+  const int cnt = C.far_skip ? A.nl_near[b.g] : A.nl_cnt[b.g];
   const long long row = C.nl_base + (long long)i * C.L;
   const int4* row4 = reinterpret_cast<const int4*>(A.nl + row);
   int4 e4n = make_int4(0, 0, 0, 0);

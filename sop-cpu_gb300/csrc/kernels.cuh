@@ -26,6 +26,7 @@ struct DevArrays {
   int* exc;           // excluded partners (sorted per bead)
   int* nl;            // neighbor-list entries
   int* nl_cnt;        // row length per bead
+  int* nl_near;       // per bead: row entries [nl_near, nl_cnt) are far (see build_slice)
   RepDev* rep;        // replica descriptors
   long long cap;      // bead capacity (SoA stride)
   unsigned long long* pairs_out;  // export buffer (i<<32|j)
@@ -63,6 +64,7 @@ struct DevArrays {
   double* en_part;
   int* en_done;
   float group_frac2;  // (grouping fraction of the trigger distance)^2; > 1 = no grouping
+  int row_bands;      // list rows keep their far entries at the end (0 = off)
 };
 
 // Bits of the engine's error word (DevArrays::err): 1 and 2 a bounded wait
@@ -79,6 +81,9 @@ struct BinHdr {
   // non-native list and pair cutoffs^2 by [bead type][partner type 1, 2], in
   // FP64 for the exact decisions and rounded to FP32 for the screen
   float rl2f[kMaxTypes][2], pl2f[kMaxTypes][2];
+  // (pair cutoff + band width)^2 in FP32: a list entry farther than this at
+  // the build is "far" and sits at the end of its row
+  float bandf[kMaxTypes][2];
   double rl2d[kMaxTypes][2], pl2d[kMaxTypes][2];
 };
 

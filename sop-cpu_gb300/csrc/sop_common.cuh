@@ -85,6 +85,9 @@ struct RepDev {
   int inlup;               // reference cadence counter (sop.cpp:100,156-165)
   int rebuild;             // rebuild requested (SKIN displacement or host)
   int near;                // SKIN displacement past the grouping fraction of the trigger
+  int wide;                // some bead moved half the band width since the last list
+                           // build: the rows' far entries must be scanned again
+  float wide2;             // (half the band width - 0.01 A)^2, set at each binning
   int out;                 // this step is an output step
   int obs_pending;         // observables of the last output step still due
   int en_after;            // energies due after this step's list build
