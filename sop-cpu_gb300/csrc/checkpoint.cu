@@ -181,7 +181,7 @@ extern "C" int sop_replica_restore(sop_engine* e, int r, const void* buf, int64_
   d.rebuild = s.rebuild; d.near = s.near; d.out = s.out; d.obs_pending = s.obs_pending;
   // the snapshot's rows carry no near / far split: scan them whole until the
   // next build (same results, the far entries' pair-list bits are 0)
-  d.wide = 1;
+  d.dmax2 = 3.0e38f;
   d.en_after = s.en_after; d.running = s.running; d.status = s.status; d.max_row = s.max_row;
   d.builds = s.builds;
   std::memcpy(d.energy, s.energy, sizeof d.energy);

@@ -968,7 +968,7 @@ static int place(sop_engine* e, const sop_prepared& P, int* replica) {
   rd.cur = 0;
   rd.inlup = 1;
   rd.active = 1;
-  rd.wide = 1;  // no band split of the rows until their first build
+  rd.dmax2 = 3.0e38f;  // no band split of the rows until their first build
   CK(cudaMemcpyAsync(e->A.rep + slot, &rd, sizeof rd, cudaMemcpyHostToDevice, e->stream));
   int rc = stage_state(e, slot, P.xyz.data(), P.vel.empty() ? nullptr : P.vel.data());
   if (rc) return rc;

@@ -402,8 +402,7 @@ __device__ void bin_replica(const DevArrays& A, int r, int src, int mode, int* s
         const double bd = 2.5 * c_ff.sigma_rep[ta][tb] + band_w;
         h.bandf[a][b] = A.row_bands ? (float)(bd * bd) : 3.0e38f;  // off: nothing is far
       }
-    const double half_w = fmax(0.5 * band_w - 0.01, 0.0);
-    R->wide2 = (float)(half_w * half_w);
+    R->band_w = (mode != SOP_LIST_NONE && A.row_bands) ? (float)band_w : 0.f;
     H = h;
   }
   __syncthreads();
@@ -969,7 +968,7 @@ __device__ void run_unit(const DevArrays& A, int4 w, BuildSmem& B, unsigned char
         R->builds += 1;
         R->rebuild = 0;
         R->near = 0;
-        R->wide = 0;
+        R->dmax2 = 0.f;
       }
       if (R->en_after) replica_energy(A, R, R->cur, red);
     }
@@ -1131,9 +1130,10 @@ struct ItemCtx {
   int pull_i, pull_j;
   unsigned seed_lo, seed_hi;
   int img;        // minimum images apply (the box itself is read per bead)
-  int far_skip;   // no bead moved half the band width since the build: rows'
-                  // far entries cannot be in the pair list and are not scanned
-  float wide2;    // squared displacement past which that stops (RepDev::wide2)
+  float band_lim; // a bead displaced less than this since the build skips its
+                  // row's far band (band width - largest displacement - 0.01 A;
+                  // <= 0: rows are scanned whole)
+  float dmax2;    // the replica's largest squared displacement (RepDev::dmax2)
 };
 
 // The box of an image-mode replica: FP32 two-float for the staged
@@ -1164,8 +1164,8 @@ __device__ __forceinline__ ItemCtx load_ctx(const DevArrays& A, int r) {
   C.amp = R->noise_amp; C.T = R->T; C.kbnd = R->kbnd; C.inv_R0sq = R->inv_R0sq; C.fang = R->fang;
   C.half_skin2 = R->half_skin2; C.pull_f = R->pull_f; C.pull_i = R->pull_i;
   C.img = R->img;
-  C.far_skip = R->mode != SOP_LIST_NONE && !R->wide;
-  C.wide2 = R->wide2;
+  C.dmax2 = R->dmax2;
+  C.band_lim = R->band_w - 0.01f - sqrtf(C.dmax2);
   C.pull_j = R->pull_j; C.seed_lo = R->seed_lo; C.seed_hi = R->seed_hi;
   // a list build of this step that failed (row overflow, grid, periodic
   // image) leaves the replica frozen: no step on incomplete lists
@@ -1402,12 +1402,12 @@ __device__ __forceinline__ void bead_tail(const DevArrays& A, const ItemCtx& C, 
         const float4 xb = A.xb[g];
         const float ex = h[0] - xb.x, ey = h[1] - xb.y, ez = h[2] - xb.z;
         const float d2 = ex * ex + ey * ey + ez * ez;
-        // (h and xb are rounded to float: a displacement within 2 ulps of the
-        // limit, or coordinates so large that 2 ulps exceed the 0.01 A slack
-        // in wide2, count as past it)
+        // the replica's largest displacement, read by the next step's band
+        // test (h and xb are rounded to float: coordinates so large that two
+        // ulps exceed the 0.01 A slack there make it unknown)
         const float ulp2 = 2.4e-7f * fmaxf(fabsf(h[0]), fmaxf(fabsf(h[1]), fabsf(h[2])));
-        if (C.far_skip && (d2 > C.wide2 || ulp2 > 0.005f))
-          A.rep[C.r].wide = 1;  // far entries are scanned from the next step
+        const float dd2 = ulp2 > 0.005f ? 3.0e38f : d2;
+        if (dd2 > C.dmax2) atomicMax(reinterpret_cast<int*>(&A.rep[C.r].dmax2), __float_as_int(dd2));
         if (C.mode == SOP_LIST_SKIN) {
           if (d2 > C.half_skin2) {
             A.rep[C.r].rebuild = 1;
@@ -1440,8 +1440,16 @@ __device__ __forceinline__ void step_bead(const DevArrays& A, const ItemCtx& C, 
   // no bead of the replica has moved half the band width since the build,
   // the row's far entries (farther than the pair cutoff plus the band width
   // at the build) cannot be in the pair list: their bits stay 0 and they are
-  // not scanned (the pair filter stays exact)
-  const int cnt = C.far_skip ? A.nl_near[b.g] : A.nl_cnt[b.g];
+  // not scanned (the pair filter stays exact).  Precisely: a far pair was at
+  // least the pair cutoff + w apart at the build and each bead moved at most
+  // its displacement since, so it stays outside the cutoff while this bead's
+  // displacement plus the replica's largest one is below w
+  int cnt = A.nl_cnt[b.g];
+  if (C.band_lim > 0.f) {
+    const float4 xb = A.xb[b.g];
+    const float ex = b.hi.x - xb.x, ey = b.hi.y - xb.y, ez = b.hi.z - xb.z;
+    if (sqrtf(ex * ex + ey * ey + ez * ez) < C.band_lim) cnt = A.nl_near[b.g];
+  }
   const long long row = C.nl_base + (long long)i * C.L;
   const int4* row4 = reinterpret_cast<const int4*>(A.nl + row);
   int4 e4n = make_int4(0, 0, 0, 0);

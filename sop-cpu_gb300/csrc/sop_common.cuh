@@ -85,9 +85,10 @@ struct RepDev {
   int inlup;               // reference cadence counter (sop.cpp:100,156-165)
   int rebuild;             // rebuild requested (SKIN displacement or host)
   int near;                // SKIN displacement past the grouping fraction of the trigger
-  int wide;                // some bead moved half the band width since the last list
-                           // build: the rows' far entries must be scanned again
-  float wide2;             // (half the band width - 0.01 A)^2, set at each binning
+  float dmax2;             // largest squared displacement of a bead since the last
+                           // list build (3e38: unknown, rows are scanned whole)
+  float band_w;            // width of the rows' far band (0: rows not banded), set at
+                           // each binning
   int out;                 // this step is an output step
   int obs_pending;         // observables of the last output step still due
   int en_after;            // energies due after this step's list build
