@@ -496,8 +496,9 @@ def single_system(args):
         r = eng.add(s, make_params(workload_script(), seed=1000))
         eng.run(50)  # warm
         tuned = None
-        if args.autotune > 0:  # launch shape for one replica (its trials are real steps)
-            report = eng.autotune(args.autotune, shape=True, lists=False)
+        if args.autotune > 0:  # launch shape for one replica (its trials are real steps,
+            # ~20 us each here, so at least 1000 per trial to rank the shapes)
+            report = eng.autotune(max(args.autotune, 1000), shape=True, lists=False)
             tuned = [l for l in report.splitlines() if l.startswith("chosen")]
         total, errs = 0.0, []
         for _ in range(windows):
