@@ -176,6 +176,14 @@ typedef struct sop_engine_config {
    * replica has moved half the band width since the build: they cannot be
    * in the pair list then.  0 = on, <0 = off (same results either way). */
   int row_bands;
+  /* Step CTAs take item blocks of about equal estimated cost
+   * (item_cost_beads >= 0) from a queue, this many blocks per CTA, rather
+   * than one fixed block each: CTAs whose items run long take fewer.  0 =
+   * automatic: the queue with one item per block while some replica is
+   * above the stage limit (its items gather through L1/L2 and cost more per
+   * bead than the split assumes), else one fixed block per CTA; <0 = one
+   * fixed block per CTA.  Same results either way. */
+  int queue_blocks;
 } sop_engine_config;
 
 /* ---- engine -------------------------------------------------------------- */

@@ -135,6 +135,7 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
       {"slice", &LaunchShape::slice, {16, 32, 64, 128}},
       {"group", &LaunchShape::group_pct, {0, 30, 50, 70}},
       {"cost", &LaunchShape::item_cost, {-1, 64, 128, 256, 512}},
+      {"queue", &LaunchShape::queue, {-1, 0, 2, 4, 8}},
   };
   const std::vector<double> skins = {1.0, 1.5, 2.0, 3.0, 4.0};
   // absolute cell edges (A); the build widens an edge below half the list
@@ -169,10 +170,11 @@ extern "C" int sop_autotune_ex(sop_engine* e, int steps_per_trial, int what, cha
   if (rc) return rc;
 
   auto describe = [](const LaunchShape& s) {
-    char buf[160];
-    snprintf(buf, sizeof buf, "threads=%d chunk=%d stage=%d slice=%d occ=%d warp=%d lanes=%d group=%d cost=%d",
+    char buf[200];
+    snprintf(buf, sizeof buf,
+             "threads=%d chunk=%d stage=%d slice=%d occ=%d warp=%d lanes=%d group=%d cost=%d queue=%d",
              s.threads, s.chunk, s.stage, s.slice, s.min_blocks, s.strategy, s.lanes, s.group_pct,
-             s.item_cost);
+             s.item_cost, s.queue);
     return std::string(buf);
   };
   LaunchShape cur = get_launch_shape(e);

@@ -314,6 +314,11 @@ static int engine_init(sop_engine* e) {
   CK(dalloc(&e->d_counts, 3));
   e->cta_first_cap = 32 * e->prop.multiProcessorCount + 1;  // any resident grid + 1
   CK(dalloc(&e->d_cta_first, e->cta_first_cap));
+  // the CTA queue: up to kMaxQueueBlocks blocks per resident CTA
+  e->blk_cap = kMaxQueueBlocks * (e->cta_first_cap - 1);
+  CK(dalloc(&A.blk, e->blk_cap));
+  CK(dalloc(&A.blk_q, 4));
+  CK(cudaMemsetAsync(A.blk_q, 0, 4 * sizeof(int), e->stream));
   CK(cudaMemsetAsync(e->d_counts, 0, 3 * sizeof(int), e->stream));
   e->items64_cap = cap / 256 + cfg.max_replicas + 16;
   CK(dalloc(&e->d_items64, e->items64_cap));
@@ -365,6 +370,7 @@ extern "C" int sop_engine_create(const sop_engine_config* cfg_in, sop_engine** o
     if (cfg_in->stage_wait_ns > 0) cfg.stage_wait_ns = std::min<int64_t>(cfg_in->stage_wait_ns, kMaxWaitNs);
     cfg.row_bands = cfg_in->row_bands < 0 ? -1 : 0;
     if (cfg_in->item_cost_beads != 0) cfg.item_cost_beads = std::min(cfg_in->item_cost_beads, 1 << 20);
+    if (cfg_in->queue_blocks != 0) cfg.queue_blocks = cfg_in->queue_blocks < 0 ? -1 : std::min(cfg_in->queue_blocks, kMaxQueueBlocks);
   }
   if (cfg.group_rebuild_pct < 0 || cfg.group_rebuild_pct >= 100) cfg.group_rebuild_pct = 0;
   if (cfg.step_strategy != 1) cfg.step_strategy = 0;
@@ -406,7 +412,7 @@ extern "C" int sop_engine_destroy(sop_engine* e) {
                   A.exc_rng, A.nl_cnt, A.nl_near, A.nl, A.nat, A.nat_r0, A.bnd, A.bnd_r0, A.ang, A.exc,
                   A.rep, A.pairs_out, A.pairs_cnt, A.err, A.units, A.unit_cnt, A.slice_done,
                   A.done_list, A.done_cnt, e->d_ids, e->d_items, e->d_items64, e->d_counts, e->d_cta_first,
-                  e->d_pack_xyz,
+                  A.blk, A.blk_q, e->d_pack_xyz,
                   e->d_pack_vel, e->d_pack_ids, e->d_pack_off, e->d_reps_pack, e->d_en_base,
                   A.en_part, A.en_done, A.bin_p, A.bin_sorted,
                   A.bin_cell, A.cstart, A.ccur, A.bin_hdr, A.step_ctr};
@@ -1389,10 +1395,37 @@ int sop::refresh_layout(sop_engine* e) {
   }
   if ((long long)e->items.size() + 64 > e->items_cap) return SOP_ERR_FULL;
   if ((long long)e->items64.size() > e->items64_cap) return SOP_ERR_FULL;
+  // the CTA queue: on request, or (automatic) while some replica steps
+  // without staging; a captured graph launched the other way is recaptured
+  bool unstaged = false;
+  for (const StepItem& w : e->items) unstaged = unstaged || !w.staged;
+  const bool queue = e->cfg.item_cost_beads >= 0 && e->step_grid <= e->cta_first_cap - 1 &&
+                     (e->cfg.queue_blocks > 0 || (e->cfg.queue_blocks == 0 && unstaged));
+  if (queue != e->step_queue) e->graph_valid = false;
+  e->step_queue = queue;
   if (e->cfg.item_cost_beads >= 0 && e->step_grid <= e->cta_first_cap - 1) {
-    split_items(e->items, e->step_grid, e->cfg.item_cost_beads, e->h_cta_first);
-    CK(h2d(e->d_cta_first, e->h_cta_first.data(), e->h_cta_first.size(), e->stream));
+    if (queue) {
+      // blocks {first, end} in item order, none empty
+      const int per_cta = e->cfg.queue_blocks > 0 ? e->cfg.queue_blocks : kMaxQueueBlocks;
+      const int nb = std::min<long long>(e->blk_cap, (long long)per_cta * e->step_grid);
+      std::vector<int> first;
+      split_items(e->items, nb, e->cfg.item_cost_beads, first);
+      e->h_blk.clear();
+      for (int b = 0; b < nb; b++)
+        if (first[b] < first[b + 1]) {
+          e->h_blk.push_back(first[b]);
+          e->h_blk.push_back(first[b + 1]);
+        }
+      const int q[4] = {0, 0, (int)(e->h_blk.size() / 2), 0};
+      if (!e->h_blk.empty())
+        CK(h2d(reinterpret_cast<int*>(e->A.blk), e->h_blk.data(), e->h_blk.size(), e->stream));
+      CK(h2d(e->A.blk_q, q, 4, e->stream));
+    } else {
+      split_items(e->items, e->step_grid, e->cfg.item_cost_beads, e->h_cta_first);
+      CK(h2d(e->d_cta_first, e->h_cta_first.data(), e->h_cta_first.size(), e->stream));
+    }
   }
+
   // the kernels read the counts from device memory, so a captured graph stays
   // valid; only the first FP64 replica (one more kernel per step) needs a recapture
   const int counts[3] = {(int)ids.size(), (int)e->items.size(), (int)e->items64.size()};
@@ -1409,9 +1442,12 @@ int sop::refresh_layout(sop_engine* e) {
 
 // Item boundaries of the batched step's CTAs, or null for equal item counts.
 static const int* cta_first(const sop_engine* e) {
-  return (e->cfg.item_cost_beads >= 0 && e->step_grid <= e->cta_first_cap - 1) ? e->d_cta_first
-                                                                              : nullptr;
+  return (e->cfg.item_cost_beads >= 0 && !e->step_queue && e->step_grid <= e->cta_first_cap - 1)
+             ? e->d_cta_first : nullptr;
 }
+// Whether the batched step's CTAs take their item blocks from the CTA queue
+// (decided by the last layout).
+static int step_queue(const sop_engine* e) { return e->step_queue ? 1 : 0; }
 
 // One step over given ids / items with host counts (single-replica paths).
 int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem* d_items,
@@ -1421,7 +1457,7 @@ int sop::enqueue_step(sop_engine* e, const int* d_ids, int nrep, const StepItem*
   if (fp64)
     CK(launch_step64(e->A, d_items, nitems, nullptr, step_grid, e->stream));
   else
-    CK(launch_step(e->A, d_items, nitems, nullptr, nullptr, max_staged, e->cfg.lanes_per_bead,
+    CK(launch_step(e->A, d_items, nitems, nullptr, nullptr, 0, max_staged, e->cfg.lanes_per_bead,
                    e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads, step_grid,
                    e->stream));
   e->launches += kStepLaunches;
@@ -1437,7 +1473,7 @@ int sop::enqueue_batched_step(sop_engine* e, bool full) {
   CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0,
                      (full || e->cfg.lean_prep < 0) ? 1 : 0,
                      e->pro_grid, e->stream));
-  CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, cta_first(e), e->max_staged,
+  CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, cta_first(e), step_queue(e), e->max_staged,
                  e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy,
                  e->cfg.block_threads, e->step_grid, e->stream));
   e->launches += kStepLaunches;
@@ -1756,6 +1792,7 @@ sop::LaunchShape sop::get_launch_shape(const sop_engine* e) {
   s.lanes = e->cfg.lanes_per_bead;
   s.group_pct = e->cfg.group_rebuild_pct;
   s.item_cost = e->cfg.item_cost_beads;
+  s.queue = e->cfg.queue_blocks;
   return s;
 }
 
@@ -1772,6 +1809,7 @@ void sop::set_launch_shape(sop_engine* e, const LaunchShape& s) {
   e->max_staged = e->cfg.stage_limit > 0 ? e->cfg.stage_limit : 0;
   e->cfg.group_rebuild_pct = (s.group_pct > 0 && s.group_pct < 100) ? s.group_pct : 0;
   e->cfg.item_cost_beads = s.item_cost < 0 ? -1 : std::min(s.item_cost, 1 << 20);
+  e->cfg.queue_blocks = s.queue < 0 ? -1 : std::min(s.queue, kMaxQueueBlocks);
   e->A.group_frac2 = e->cfg.group_rebuild_pct > 0
                          ? (float)(1e-4 * e->cfg.group_rebuild_pct * e->cfg.group_rebuild_pct)
                          : 4.0f;
@@ -1817,7 +1855,7 @@ extern "C" int sop_profile_steps_ex(sop_engine* e, int64_t nsteps, double* ms) {
     CK(launch_prologue(e->A, e->d_ids, e->cfg.max_replicas, e->d_counts, 0, 0, s == 0, e->pro_grid,
                        e->stream, E[1], E[2]));
     CK(cudaEventRecord(E[3], e->stream));
-    CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, cta_first(e), e->max_staged,
+    CK(launch_step(e->A, e->d_items, (int)e->items_cap, e->d_counts + 1, cta_first(e), step_queue(e), e->max_staged,
                    e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy, e->cfg.block_threads, e->step_grid, e->stream));
     CK(cudaEventRecord(E[4], e->stream));
     e->launches += kStepLaunches;
@@ -1942,7 +1980,7 @@ static int run_phase(sop_engine* e, int r, int phase) {
   if (R.params.precision == SOP_PREC_FP64)
     CK(launch_step64(e->A, e->d_items + item_slot, (int)items.size(), nullptr, grid, e->stream));
   else
-    CK(launch_step(e->A, e->d_items + item_slot, (int)items.size(), nullptr, nullptr, staged ? R.n : 0,
+    CK(launch_step(e->A, e->d_items + item_slot, (int)items.size(), nullptr, nullptr, 0, staged ? R.n : 0,
                    e->cfg.lanes_per_bead, e->cfg.step_min_blocks, e->cfg.step_strategy,
                    e->cfg.block_threads, grid, e->stream));
   e->launches += 2;

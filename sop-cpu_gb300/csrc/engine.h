@@ -62,6 +62,7 @@ struct NvtxRange {
 
 constexpr int64_t kDefaultWaitNs = 2000000000LL;  // device-side wait limits: 2 s
 constexpr int64_t kMaxWaitNs = 60000000000LL;
+constexpr int kMaxQueueBlocks = 8;  // item blocks per step CTA in the CTA queue (at most)
 
 struct sop_engine {
   sop_engine_config cfg{};
@@ -93,6 +94,9 @@ struct sop_engine {
   int* d_cta_first = nullptr;       // per step CTA, its first work item (cost-balanced split)
   int cta_first_cap = 0;
   std::vector<int> h_cta_first;
+  long long blk_cap = 0;            // CTA queue blocks (DevArrays::blk)
+  bool step_queue = false;          // the batched step's CTAs take blocks from the queue
+  std::vector<int> h_blk;
   // packed host-order state of sop_run_host (one copy each way)
   double* d_pack_xyz = nullptr;
   double* d_pack_vel = nullptr;
@@ -136,6 +140,7 @@ struct LaunchShape {
   int lanes;       // lanes per bead
   int group_pct;   // grouped skin rebuilds (0 = off)
   int item_cost;   // step CTA blocks by estimated cost (bead equivalents per item; <0 = equal counts)
+  int queue;       // item blocks per CTA in the CTA queue (0 = automatic, <0 = one fixed block per CTA)
 };
 LaunchShape get_launch_shape(const sop_engine* e);
 // recompute the persistent grid, invalidate layout and graph

@@ -1519,6 +1519,7 @@ __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* i
   extern __shared__ __align__(128) float4 sst[];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ ItemCtx sC;
+  __shared__ int s_block;
   const int lane = threadIdx.x & (G - 1);
   const int grp = threadIdx.x / G, ngrp = blockDim.x / G;
   const unsigned gmask =
@@ -1527,16 +1528,40 @@ __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* i
   fence_async_smem();
   __syncthreads();
   uint32_t parity = 0;
-  // a contiguous block of items per CTA: [cta_first[b], cta_first[b + 1])
-  // when the host split the items by estimated cost, else equal item counts;
-  // consecutive items of one replica merge into one bead range, staged once,
-  // with no barrier inside it.  (A CTA's time is set by its chain of items,
-  // each with a fixed staging and row-latency cost on top of its beads.)
-  const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int it0 = cta_first ? min(nitems, cta_first[blockIdx.x]) : (int)blockIdx.x * per;
-  const int it_end = cta_first ? min(nitems, cta_first[blockIdx.x + 1])
-                               : min(nitems, ((int)blockIdx.x + 1) * per);
-  for (int it = it0; it < it_end;) {
+  // The CTA's work items: one contiguous block [cta_first[b], cta_first[b + 1])
+  // when the host split the items by estimated cost (else equal item counts),
+  // or (blk_dyn) blocks of about equal estimated cost: CTA b's first block is
+  // block b, and the blocks past the grid are taken in turn from the queue
+  // blk_q = {next block, CTAs done, blocks}, so that CTAs whose rows run
+  // short take more of them; the last CTA to finish resets the queue for the
+  // next launch.  Consecutive items of one replica merge into one bead range,
+  // staged once.  (A CTA's time is set by its chain of items, each with a
+  // fixed staging and row-latency cost on top of its beads.)
+  const bool dyn = A.blk_dyn != 0;
+  bool first = true;
+  int it = 0, it_end = 0;
+  if (!dyn) {
+    const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
+    it = cta_first ? min(nitems, cta_first[blockIdx.x]) : (int)blockIdx.x * per;
+    it_end = cta_first ? min(nitems, cta_first[blockIdx.x + 1]) : min(nitems, ((int)blockIdx.x + 1) * per);
+  }
+  for (;;) {
+    if (it >= it_end) {
+      if (!dyn) break;
+      int k = (int)blockIdx.x;
+      if (!first) {
+        if (threadIdx.x == 0) s_block = (int)gridDim.x + atomicAdd(A.blk_q, 1);
+        __syncthreads();
+        k = s_block;
+        __syncthreads();  // s_block is rewritten by the next take
+      }
+      first = false;
+      if (k >= A.blk_q[2]) break;
+      const int2 bk = A.blk[k];
+      it = min(nitems, bk.x);
+      it_end = min(nitems, bk.y);
+      continue;
+    }
     StepItem w = items[it];
     int nx = it + 1;
     for (; nx < it_end; ++nx) {
@@ -1579,7 +1604,7 @@ __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* i
           const unsigned long long t1 = globaltimer_ns();
           while (!mbar_try_wait(&mbar, parity) && globaltimer_ns() - t1 < kDrainNs) {
           }
-          return;
+          break;
         }
         parity ^= 1u;
         if (C.img)
@@ -1595,6 +1620,16 @@ __global__ void __launch_bounds__(TPB, MB) k_step(DevArrays A, const StepItem* i
       }
     }
     __syncthreads();
+  }
+  // every CTA passes here (a late staging copy included), so the queue is
+  // reset once all CTAs have taken their last block
+  if (dyn && threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(A.blk_q + 1, 1) == (int)gridDim.x - 1) {
+      A.blk_q[0] = 0;
+      A.blk_q[1] = 0;
+      __threadfence();
+    }
   }
 }
 
@@ -2261,13 +2296,15 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, co
 }
 
 cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
-                        const int* cta_first, int max_staged, int lanes, int min_blocks,
+                        const int* cta_first, int queue, int max_staged, int lanes, int min_blocks,
                         int strategy, int threads, int grid, cudaStream_t s) {
   if (nitems <= 0) return cudaSuccess;
   const size_t dyn = strategy == 1 ? 0 : (size_t)max_staged * 32 + 128;
   if (grid <= 0) grid = nitems;
   if (!step_shape_supported(lanes, strategy, threads)) return cudaErrorInvalidConfiguration;
-  step_kernel(lanes, min_blocks, strategy, threads)<<<grid, threads, dyn, s>>>(A, items, nitems_dev,
+  DevArrays B = A;
+  B.blk_dyn = (queue && strategy != 1) ? 1 : 0;
+  step_kernel(lanes, min_blocks, strategy, threads)<<<grid, threads, dyn, s>>>(B, items, nitems_dev,
                                                                               nitems, cta_first);
   return cudaGetLastError();
 }

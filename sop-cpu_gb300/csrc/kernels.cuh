@@ -65,6 +65,11 @@ struct DevArrays {
   int* en_done;
   float group_frac2;  // (grouping fraction of the trigger distance)^2; > 1 = no grouping
   int row_bands;      // list rows keep their far entries at the end (0 = off)
+  // k_step's CTA queue: blocks of work items {first, end} that the CTAs take
+  // in turn when blk_dyn is set; blk_q = {next block, CTAs done, blocks}
+  int2* blk;
+  int* blk_q;
+  int blk_dyn;
 };
 
 // Bits of the engine's error word (DevArrays::err): 1 and 2 a bounded wait
@@ -130,8 +135,10 @@ cudaError_t launch_prologue(const DevArrays& A, const int* rep_ids, int nrep, co
 // tasks gathering through L1/L2 (k_step_w); bit-identical results
 // cta_first: grid + 1 item boundaries, CTA b steps items [cta_first[b],
 // cta_first[b + 1]) (the CTA strategy; null = equal item counts)
+// queue: the CTAs take item blocks from A.blk / A.blk_q instead (the CTA
+// strategy; the blocks index `items`)
 cudaError_t launch_step(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,
-                        const int* cta_first, int max_staged, int lanes, int min_blocks,
+                        const int* cta_first, int queue, int max_staged, int lanes, int min_blocks,
                         int strategy, int threads, int grid, cudaStream_t s);
 // the FP64-precision step over its own items (one thread per bead)
 cudaError_t launch_step64(const DevArrays& A, const StepItem* items, int nitems, const int* nitems_dev,

@@ -84,6 +84,7 @@ class EngineConfig(C.Structure):
         ("step_min_blocks", C.c_int), ("step_strategy", C.c_int), ("group_rebuild_pct", C.c_int),
         ("lean_prep", C.c_int), ("queue_wait_ns", C.c_int64), ("stage_wait_ns", C.c_int64),
         ("item_cost_beads", C.c_int), ("row_bands", C.c_int),
+        ("queue_blocks", C.c_int),
     ]
 
 

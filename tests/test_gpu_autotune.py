@@ -82,6 +82,9 @@ def test_list_tuning_keeps_reference_pair_sets():
                                  dict(step_min_blocks=3, stage_limit=2048), dict(step_min_blocks=2),
                                  dict(stage_limit=-1), dict(build_slice_beads=128, chunk_beads=64),
                                  dict(item_cost_beads=-1), dict(item_cost_beads=16, chunk_beads=64),
+                                 dict(queue_blocks=-1), dict(queue_blocks=8, chunk_beads=32),
+                                 dict(queue_blocks=1, lanes_per_bead=1, block_threads=512),
+                                 dict(queue_blocks=2, stage_limit=-1),
                                  dict(lanes_per_bead=4), dict(lanes_per_bead=1), dict(block_threads=64),
                                  dict(block_threads=128, lanes_per_bead=4, chunk_beads=512),
                                  dict(group_rebuild_pct=-1), dict(group_rebuild_pct=90),
@@ -90,8 +93,8 @@ def test_list_tuning_keeps_reference_pair_sets():
                                  dict(block_threads=512, lanes_per_bead=4, stage_limit=-1)])
 def test_launch_shapes_bit_identical(cfg):
     """Every launch shape, both step strategies (CTA items staged in shared
-    memory, warp tasks through L1/L2), every lane count and rebuild grouping
-    give the same trajectories: each force is an exact integer sum of its
+    memory, warp tasks through L1/L2), fixed or queued CTA blocks, every lane
+    count and rebuild grouping give the same trajectories: each force is an exact integer sum of its
     pair contributions, whatever the list order or the build times."""
     systems = [S.synth_chain(8400 + k, n) for k, n in enumerate([60, 700, 2600, 5000, 130])]
     params = [make_params(script(), seed=4400 + k, list_mode="skin" if k % 2 else "neighborlist",
