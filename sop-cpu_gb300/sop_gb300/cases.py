@@ -9,6 +9,9 @@ single-kernel captures).  Run as
 mix      512 replicas, N log-uniform 30-1500 (seed 2000), T 0.4-0.9, skin lists
          (3.0 A): the batched step workload; one CUDA-graph-free batched step
          per --steps.
+mixwide  the same with 384 replicas, N log-uniform 30-5000: the serving mix,
+         74 replicas above the stage limit (the CTA queue on, unless
+         --queue-blocks -1).
 build    one 1500-bead chain, neighbor list rebuilt before every step (nnlup 1):
          every prologue is a full list build.
 mixbuild the mix with the reference's neighbor-list cadence at nnlup 1: every
@@ -66,13 +69,18 @@ def globule_engine(nchain=100, chain_len=500, skin=2.0):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("case", choices=("mix", "mixbuild", "build", "globule"))
+    ap.add_argument("case", choices=("mix", "mixwide", "mixbuild", "build", "globule"))
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warm", type=int, default=10, help="batched steps before the profiled ones")
     ap.add_argument("--tune", type=int, default=0,
                     help="autotune with this many steps per trial before profiling")
+    ap.add_argument("--queue-blocks", type=int, default=0,
+                    help="the engine's queue_blocks (0: automatic, <0: fixed CTA blocks)")
     a = ap.parse_args(argv)
-    eng, systems = {"mix": mix_engine, "mixbuild": lambda: mix_engine(every_step=True),
+    q = a.queue_blocks
+    eng, systems = {"mix": lambda: mix_engine(queue_blocks=q),
+                    "mixwide": lambda: mix_engine(count=384, lo=30, hi=5000, queue_blocks=q),
+                    "mixbuild": lambda: mix_engine(every_step=True, queue_blocks=q),
                     "build": build_engine, "globule": globule_engine}[a.case]()
     if a.warm:
         eng.run(a.warm)
