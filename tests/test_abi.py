@@ -43,6 +43,21 @@ def test_version_and_defaults():
     assert c.lanes_per_bead in (1, 2, 4, 8, 16) and c.block_threads % 32 == 0
 
 
+@pytest.mark.parametrize("fill,struct", [("sop_engine_config_default", L.EngineConfig),
+                                         ("sop_params_default", L.Params)])
+def test_struct_bindings_match_the_library(fill, struct):
+    """The library's default filler clears its whole struct before setting
+    fields, so it writes exactly sizeof(struct) bytes: a binding that is
+    shorter than the C struct shows as an overwritten sentinel after it, one
+    that is longer as sentinel bytes left inside it (no default holds 0xAB)."""
+    n = C.sizeof(struct)
+    buf = (C.c_ubyte * (n + 64))(*([0xAB] * (n + 64)))
+    getattr(L.lib(), fill)(C.cast(buf, C.POINTER(struct)))
+    raw = bytes(buf)
+    assert raw[n:] == b"\xab" * 64
+    assert 0xAB not in raw[:n]
+
+
 def _split(x):
     hi, lo = C.c_float(), C.c_float()
     L.lib().sop_selftest_split(C.c_double(x), C.byref(hi), C.byref(lo))
