@@ -188,6 +188,11 @@ typedef struct sop_engine_config {
 
 /* ---- engine -------------------------------------------------------------- */
 const char* sop_version(void);
+/* sizeof one of this header's structs by name ("sop_params",
+ * "sop_system_desc", "sop_engine_config", "sop_server_config",
+ * "sop_request_result"), or -1 for any other name: a binding in another
+ * language checks its struct layouts against the library it loaded. */
+int sop_struct_size(const char* name);
 const char* sop_status_string(int status);
 void sop_params_default(sop_params* p);   /* params.cpp:262-400 defaults      */
 void sop_engine_config_default(sop_engine_config* c);

@@ -125,6 +125,17 @@ static char g_last_error[512];
 
 extern "C" const char* sop_version(void) { return "sop-gb300 1.0 (sm_103a)"; }
 
+extern "C" int sop_struct_size(const char* name) {
+  if (!name) return -1;
+  const std::string n(name);
+  if (n == "sop_params") return (int)sizeof(sop_params);
+  if (n == "sop_system_desc") return (int)sizeof(sop_system_desc);
+  if (n == "sop_engine_config") return (int)sizeof(sop_engine_config);
+  if (n == "sop_server_config") return (int)sizeof(sop_server_config);
+  if (n == "sop_request_result") return (int)sizeof(sop_request_result);
+  return -1;
+}
+
 extern "C" const char* sop_status_string(int s) {
   switch (s) {
     case SOP_OK: return "ok";

@@ -107,6 +107,7 @@ class RequestResult(C.Structure):
 VP = C.c_void_p
 _PROTOS = {
     "sop_version": (C.c_char_p, []),
+    "sop_struct_size": (C.c_int, [C.c_char_p]),
     "sop_status_string": (C.c_char_p, [C.c_int]),
     "sop_params_default": (None, [C.POINTER(Params)]),
     "sop_engine_config_default": (None, [C.POINTER(EngineConfig)]),
@@ -192,6 +193,10 @@ def lib():
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
+        wrong = ["%s (library %d bytes, binding %d)" % (n, L.sop_struct_size(n.encode()), C.sizeof(s))
+                 for n, s in STRUCTS.items() if L.sop_struct_size(n.encode()) != C.sizeof(s)]
+        if wrong:
+            raise RuntimeError("struct layouts differ from %s: %s" % (LIB_PATH, "; ".join(wrong)))
         _lib = L
     return _lib
 
@@ -200,6 +205,11 @@ def check(code, where):
     if code != SOP_OK:
         raise SopError(code, where)
     return code
+
+
+# the header's structs and their bindings (checked against the library at load)
+STRUCTS = {"sop_params": Params, "sop_system_desc": SystemDesc, "sop_engine_config": EngineConfig,
+           "sop_server_config": ServerConfig, "sop_request_result": RequestResult}
 
 
 def exported_symbols():

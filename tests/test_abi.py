@@ -58,6 +58,17 @@ def test_struct_bindings_match_the_library(fill, struct):
     assert 0xAB not in raw[:n]
 
 
+@pytest.mark.parametrize("name", ["sop_params", "sop_system_desc", "sop_engine_config",
+                                  "sop_server_config", "sop_request_result"])
+def test_struct_sizes_match_the_library(name):
+    assert L.lib().sop_struct_size(name.encode()) == C.sizeof(L.STRUCTS[name])
+
+
+def test_struct_size_of_other_names():
+    assert L.lib().sop_struct_size(b"sop_engine") == -1
+    assert L.lib().sop_struct_size(None) == -1
+
+
 def _split(x):
     hi, lo = C.c_float(), C.c_float()
     L.lib().sop_selftest_split(C.c_double(x), C.byref(hi), C.byref(lo))
