@@ -179,10 +179,11 @@ typedef struct sop_engine_config {
   /* Step CTAs take item blocks of about equal estimated cost
    * (item_cost_beads >= 0) from a queue, this many blocks per CTA, rather
    * than one fixed block each: CTAs whose items run long take fewer.  0 =
-   * automatic: the queue with one item per block while some replica is
-   * above the stage limit (its items gather through L1/L2 and cost more per
-   * bead than the split assumes), else one fixed block per CTA; <0 = one
-   * fixed block per CTA.  Same results either way. */
+   * automatic: the queue with 8 blocks per CTA (one item each while the
+   * layout has at most 8 items per CTA) while some replica is above the
+   * stage limit (its items gather through L1/L2 and cost more per bead than
+   * the split assumes), else one fixed block per CTA; <0 = one fixed block
+   * per CTA.  Same results either way. */
   int queue_blocks;
 } sop_engine_config;
 
